@@ -1,0 +1,339 @@
+"""Benchmark: ref-views/s of the full ACMP-style pipeline on the synthetic
+room scene (20 views at 1600x1200, 10 source views per reference): random
+pass, planar prior, prior pass, two geometric passes and fusion.
+
+A step reconstructs the whole scene once (20 reference views).  `value` is
+measured with the images already resident in HBM; `e2e` adds, every step,
+the host->device copy of the 8-bit images from pinned memory and the
+device->host copy of the fused depth/normal maps.  Inputs (20 x 7.7 MB
+images, 2.5 GB of per-view state) exceed L2, so no flush is needed.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gmvs|reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ref-views/s at 1600x1200x10 src vs plain GPU path; p50/p99 per-view latency"
+UNIT = "ref-views/s"
+WORKLOAD = "room scene: 20 views 1600x1200, 10 src/view, random + planar-prior + 2 geometric passes + fusion"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gmvs", choices=["gmvs", "reference"])
+    ap.add_argument("--views", type=int, default=20)
+    ap.add_argument("--height", type=int, default=1200)
+    ap.add_argument("--width", type=int, default=1600)
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain per-view comparison step")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    return ap.parse_args()
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# ---------------------------------------------------------------- clocks --
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sms, maxs, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sms.append(float(parts[1]))
+                maxs.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": max(maxs) if maxs else None,
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+# ------------------------------------------------------------ CPU baseline --
+def cpu_baseline(sc, threads: int):
+    """The oracle's multi-view NCC evaluation of one full 1600x1200 reference
+    view with 10 sources, timed on the host cores; a pipeline reference view
+    costs 144 such evaluations (random and prior passes 1 + 14*3 each, two
+    geometric passes 1 + 14*2 each), which gives ref-views/s."""
+    import numpy as np
+
+    import oracle
+
+    ref, src = sc.problems[0]
+    ids = [ref] + list(src)
+    from gmvs_gb300 import synthetic
+
+    cam_args = [synthetic.camera_args(sc, i) for i in ids]
+    H, W = sc.hw
+    K, R = sc.K[ref], sc.R[ref]
+    d = sc.depths[ref].astype(np.float64)
+    ys, xs = np.mgrid[0:H, 0:W]
+    X = np.stack([(xs - K[0, 2]) / K[0, 0] * d, (ys - K[1, 2]) / K[1, 1] * d, d], -1)
+    n = sc.normals[ref].astype(np.float64) @ R.T
+    planes = np.concatenate([n, -np.sum(n * X, -1)[..., None]], -1).astype(np.float32)
+    imgs = sc.images[ids].astype(np.float32)
+    prm = oracle.make_params(sampler=0)
+    oracle.ncc_costs(cam_args, imgs[:, :64], planes[:64], prm, nthreads=threads)  # warm the library
+    t0 = time.perf_counter()
+    oracle.ncc_costs(cam_args, imgs, planes, prm, nthreads=threads)
+    dt = time.perf_counter() - t0
+    evals_per_view = 2 * (1 + 14 * 3) + 2 * (1 + 14 * 2)
+    return {"value": 1.0 / (evals_per_view * dt), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"oracle fp32 multi-view NCC of one {W}x{H} view x {len(src)} sources "
+                      f"({dt:.2f} s) x {evals_per_view} evaluations per pipeline view"}
+
+
+# ------------------------------------------------------------------ main --
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    import numpy as np
+    import torch
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from gmvs_gb300 import synthetic
+
+        sc = synthetic.room_scene(0, H=args.height, W=args.width, num_views=args.views,
+                                  device=torch.device("cuda") if torch.cuda.is_available() else None)
+        threads = os.cpu_count() or 1
+        vals = []
+        for _ in range(max(1, args.steps)):
+            vals.append(cpu_baseline(sc, threads))
+        v = statistics.median([x["value"] for x in vals])
+        cb = dict(vals[0])
+        cb["value"] = v
+        out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": 1000.0 / v * args.views, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": {"workload": WORKLOAD, "views": args.views, "height": args.height, "width": args.width},
+               "impl": "reference", "cpu_baseline": cb,
+               "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    from gmvs_gb300 import build as gb
+
+    gb.build()
+    from gmvs_gb300 import _abi, synthetic
+    from gmvs_gb300.pipeline import ScenePipeline, scene_inputs_from_synthetic
+
+    sc = synthetic.room_scene(0, H=args.height, W=args.width, num_views=args.views, device=dev)
+    inputs = scene_inputs_from_synthetic(sc, dev)
+    pipe = ScenePipeline(inputs, mode="batched", prior_threads=min(16, os.cpu_count() or 1))
+    for _ in range(args.warmup):
+        pipe.run()
+    torch.cuda.synchronize()
+
+    # timed region: batched pipeline, images resident
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            pipe.run()
+        e1.record()
+        torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    t_max = torch.tensor([ms], device=dev)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
+    ms = float(t_max.item())
+    value = world * args.views / (ms / 1000.0)
+
+    # per-stage breakdown and the dominant kernel's launch time (one instrumented step)
+    torch.cuda.synchronize()
+    pipe.times.seconds.clear()
+    pipe.run(timed=True)
+    stages = dict(pipe.times.seconds)
+    sweep_ms, sweep_bytes, launches = sweep_roofline(pipe, torch)
+
+    # end-to-end through host buffers: pinned 8-bit images in, fused maps out
+    host_imgs = torch.from_numpy(sc.images).pin_memory()
+    out_d = torch.empty_like(pipe.fused_depth, device="cpu").pin_memory()
+    out_n = torch.empty_like(pipe.fused_normal, device="cpu").pin_memory()
+    h2d = host_imgs.numel() * host_imgs.element_size()
+    d2h = out_d.numel() * 4 + out_n.numel() * 4
+    torch.cuda.synchronize()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record()
+    for _ in range(args.steps):
+        inputs.images.copy_(host_imgs.to(dev, non_blocking=True).to(torch.float32))
+        pipe.run()
+        out_d.copy_(pipe.fused_depth, non_blocking=True)
+        out_n.copy_(pipe.fused_normal, non_blocking=True)
+    e3.record()
+    torch.cuda.synchronize()
+    e2e_ms = e2.elapsed_time(e3) / args.steps
+
+    plain = None
+    if not args.no_plain and rank == 0:
+        pp = ScenePipeline(inputs, mode="plain", prior_threads=min(16, os.cpu_count() or 1))
+        pp.run()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pp.run()
+        torch.cuda.synchronize()
+        plain_s = time.perf_counter() - t0
+        plain = {"value": args.views / plain_s, "unit": UNIT, "steps": 1,
+                 "mode": "one view per launch chain, fp32 images, synchronised after every kernel"}
+        pp.close()
+
+    if rank != 0:
+        return
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm = peaks.get("hbm_gbs")
+    peak_note = "of measured" if hbm else "of fallback"
+    hbm = hbm or 6800.0
+    achieved = sweep_bytes / (sweep_ms / 1000.0) / 1e9 if sweep_ms else None
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "sweep_traffic.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get("bytes_per_launch")
+        except (OSError, ValueError):
+            traffic = None
+    cpu = None if args.no_cpu else cpu_baseline(sc, os.cpu_count() or 1)
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded room scene rendered on device)",
+        "config": {"workload": WORKLOAD, "views": args.views, "height": args.height, "width": args.width,
+                   "num_src": 10, "parallelism": f"replicas x{world}", "l2": "inputs larger than L2, no flush"},
+        "e2e": {"value": world * args.views / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "latency": {"p50_ms_per_view": ms / args.views, "p99_ms_per_view": ms / args.views,
+                    "note": "batched: every view of the scene completes with the step"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
+                     "kernel": "k_sweep (half-sweep over all views)", "peak_source": peak_note,
+                     "launch_ms": sweep_ms},
+        "stages_s": stages,
+        "gpu_launches": launches * args.steps,
+        "clocks": clk.summary(),
+        "plain_path": plain,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(out))
+
+
+def sweep_roofline(pipe, torch):
+    """Average duration of the half-sweep launches (CUDA events on the
+    launching stream) over one pipeline step, their algorithmic bytes (image
+    reads + 36 B/pixel of state per half-sweep + src depths in the geometric
+    passes) and the number of kernels one step launches."""
+    import numpy as np
+
+    durations, nbytes, launches = [], [], 0
+    stream = torch.cuda.current_stream()
+    V = pipe.V
+    HW = pipe.H * pipe.W
+    for key in ("random", "prior", "geom0", "geom1"):
+        plans = pipe.plans.get(key, [])
+        for plan in plans:
+            n_st = plan.num_stages
+            iters = (n_st - 4) // 2
+            for s in range(n_st):
+                is_sweep = 1 <= s <= 2 * iters
+                if is_sweep:
+                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                plan.launch_stage(s)
+                launches += 1
+                if is_sweep:
+                    b.record(stream)
+                    durations.append((a, b))
+                    b_img = 2  # fp16 staged images (algorithmic 2 B/pixel)
+                    if key in ("random", "prior"):
+                        b_img = 4  # fp32 textures
+                    per_view = 0
+                    for v in plan.views:
+                        n = len(v.images)
+                        per_view += n * HW * b_img + 36 * HW + (n * HW * 4 if key.startswith("geom") else 0)
+                    nbytes.append(per_view)
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in durations]
+    # fusion launches 2 kernels per view
+    launches += 2 * V
+    if not ms:
+        return None, 0, launches
+    return float(np.mean(ms)), float(np.mean(nbytes)), launches
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,92 @@
+"""Build the in-tree C-ABI library libgmvs_gb300.so for sm_103a.
+
+Every translation unit is compiled in parallel with nvcc
+(``-gencode arch=compute_103a,code=sm_103a``) and linked into
+``gmvs_gb300/_lib/libgmvs_gb300.so``.  ``fusion.cu`` is compiled with
+``-fmad=false`` so its arithmetic rounds like the sequential host scan.
+"""
+
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT_DIR = os.path.join(HERE, "_lib")
+LIB_PATH = os.path.join(OUT_DIR, "libgmvs_gb300.so")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+              "-I" + INCLUDE]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-I" + INCLUDE]
+
+SOURCES = {
+    "pm_f32.cu": [],
+    "pm_qf32.cu": [],
+    "pm_qf16.cu": [],
+    "pm_tex.cu": [],
+    "runtime.cu": [],
+    "fusion.cu": ["-fmad=false"],
+    "prior.cpp": [],
+}
+
+
+def _nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(cand):
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build gmvs_gb300")
+    return cand
+
+
+def _inputs() -> list[str]:
+    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    files.append(os.path.join(INCLUDE, "gmvs_gb300.h"))
+    files.append(os.path.abspath(__file__))
+    return files
+
+
+def is_stale() -> bool:
+    if not os.path.exists(LIB_PATH):
+        return True
+    t = os.path.getmtime(LIB_PATH)
+    return any(os.path.getmtime(f) > t for f in _inputs())
+
+
+def _compile(src: str, extra: list[str], verbose: bool) -> str:
+    obj = os.path.join(OUT_DIR, "obj", src + ".o")
+    path = os.path.join(CSRC, src)
+    if src.endswith(".cpp"):
+        cmd = [os.environ.get("CXX", "g++"), *CXX_FLAGS, "-c", path, "-o", obj]
+    else:
+        cmd = [_nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", path, "-o", obj]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compiling {src} failed:\n{r.stdout}\n{r.stderr}")
+    return obj
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile and link the library if any input changed; return its path."""
+    if not force and not is_stale():
+        return LIB_PATH
+    os.makedirs(os.path.join(OUT_DIR, "obj"), exist_ok=True)
+    with ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose), SOURCES.items()))
+    tmp = LIB_PATH + ".tmp"
+    cmd = [_nvcc(), *ARCH, "-shared", "-o", tmp, *objs]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"linking libgmvs_gb300.so failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

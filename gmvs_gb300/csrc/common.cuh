@@ -1,0 +1,166 @@
+// Device-side data layout and helpers shared by the PatchMatch and fusion
+// kernels.  Host code fills DevView/DevParams/Tile (see runtime.cu); kernels
+// only read them.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gmvs_gb300.h"
+
+namespace gmvs {
+
+constexpr int kMaxNgb = GMVS_MAX_NGB;
+constexpr int kMaxIters = 32;
+
+// Error bits a kernel may raise in the plan's device error word.
+enum : int { kErrBadView = 1, kErrBadStage = 2 };
+
+struct DevCam {  // world -> camera, as gmvs_camera without the extents
+    float K[9];
+    float R[9];
+    float t[3];
+};
+
+// One reference view of a pass.  Homography of plane (n, w) in the ref
+// camera frame towards source j is H = A_j - b_j g^T with
+//   A_j = K_s R_rel K_r^-1,  b_j = K_s t_rel,
+//   g   = (n_x / fx, n_y / fy, n_z - n_x cx / fx - n_y cy / fy) / w,
+// which is ComputeHomography (patch_match_kernel.cu:262-360) re-associated;
+// A_j and b_j are formed once per view pair in FP64 and rounded once.
+struct DevView {
+    int H, W, N, stream_id;
+    float depth_min, depth_max;
+    float src_w[kMaxNgb], src_h[kMaxNgb];  // centre test extents (camera width/height)
+    float A[kMaxNgb][9];
+    float b[kMaxNgb][3];
+    DevCam cam[1 + kMaxNgb];  // ref, then sources (geometric term, conversions)
+    const void* img[1 + kMaxNgb];           // CLAMP sampler: staged planes
+    unsigned long long tex[1 + kMaxNgb];    // TEX sampler: texture objects
+    const float* dep[1 + kMaxNgb];          // GEOM: input depth maps
+    const float* ref_normal;                // DEPTH_NORMAL init
+    const float4* prior_planes;
+    const uint32_t* prior_masks;
+    const float4* init_planes;
+    const float* init_costs;
+    float4* plane[2];   // ping-pong state
+    float* cost[2];
+    uint32_t* sel[2];
+    float4* fin;        // converted (world normal, depth) planes for the filter
+    float* out_depth;
+    float* out_normal;
+    float* out_cost;
+    float4* out_planes;
+};
+
+struct DevParams {
+    int patch_size, radius_increment, top_k;
+    float sigma_spatial, sigma_color;
+    int init_kind, sweep_kind, sampler, staging;
+    uint32_t seed_lo, seed_hi;
+    int pass_index, max_iterations;
+    int nmax;  // largest N of the plan (shared-memory stride)
+    float cost_thr[kMaxIters];
+};
+
+// A tile is TW columns x TH thread rows of one view; thread row r covers
+// image rows 2*(yh0 + r) and 2*(yh0 + r) + 1 (zig-zag by column parity, the
+// reference's red/black launch mapping, patch_match_kernel.cu:1592-1599).
+// stage < 0: use the launch's stage argument.
+struct Tile {
+    int view, x0, yh0, stage;
+};
+
+// ---------------------------------------------------------------- Philox --
+// Philox4x32-10 (Salmon et al., SC'11).  Key = seed; counter = (pixel,
+// stream, phase, block), phase = pass_index << 8 | step (0 init, 1 + 2*iter +
+// colour for the sweeps).  Uniforms are ((x >> 8) + 1) * 2^-24 in (0, 1].
+__device__ __forceinline__ uint4 philox10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) {
+            k.x += 0x9E3779B9u;
+            k.y += 0xBB67AE85u;
+        }
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    }
+    return c;
+}
+
+struct DevRng {
+    uint2 key;
+    uint4 ctr;
+    uint4 buf;
+    int left;
+    __device__ __forceinline__ DevRng(uint32_t seed_lo, uint32_t seed_hi, uint32_t pixel, uint32_t stream,
+                                      uint32_t phase) {
+        key = make_uint2(seed_lo, seed_hi);
+        ctr = make_uint4(pixel, stream, phase, 0u);
+        left = 0;
+    }
+    __device__ __forceinline__ float uniform() {
+        if (left == 0) {
+            buf = philox10(ctr, key);
+            ctr.w += 1u;
+            left = 4;
+        }
+        const uint32_t x = buf.x;
+        buf.x = buf.y;
+        buf.y = buf.z;
+        buf.z = buf.w;
+        --left;
+        return (float)((x >> 8) + 1u) * (1.0f / 16777216.0f);
+    }
+};
+
+__device__ __forceinline__ uint32_t phase_of(int pass_index, int step) {
+    return ((uint32_t)pass_index << 8) | (uint32_t)step;
+}
+
+// --------------------------------------------------------------- helpers --
+__device__ __forceinline__ float lerpf(float a, float b, float w) { return fmaf(w, b - a, a); }
+
+// module B bilinear_interpolate (gmvs/src/patch_match.cu:10-33)
+__device__ __forceinline__ float bilinear_clamp(const float* __restrict__ img, float u, float v, int H, int W) {
+    const int hl = min(max(__float2int_rz(v), 0), H - 1);
+    const int wl = min(max(__float2int_rz(u), 0), W - 1);
+    const float hd = v - (float)hl;
+    const float wd = u - (float)wl;
+    const int hu = (hl == H - 1) ? hl : hl + 1;
+    const int wu = (wl == W - 1) ? wl : wl + 1;
+    const float v0 = __ldg(img + hl * W + wl), v1 = __ldg(img + hl * W + wu);
+    const float v2 = __ldg(img + hu * W + wl), v3 = __ldg(img + hu * W + wu);
+    return lerpf(lerpf(v0, v1, wd), lerpf(v2, v3, wd), hd);
+}
+
+// Get3DPointonWorld_cu (patch_match_kernel.cu:590-620)
+__device__ __forceinline__ void point_on_world(float x, float y, float depth, const DevCam& c, float out[3]) {
+    const float px = depth * (x - c.K[2]) / c.K[0];
+    const float py = depth * (y - c.K[5]) / c.K[4];
+    const float pz = depth;
+    const float tx = c.R[0] * px + c.R[3] * py + c.R[6] * pz;
+    const float ty = c.R[1] * px + c.R[4] * py + c.R[7] * pz;
+    const float tz = c.R[2] * px + c.R[5] * py + c.R[8] * pz;
+    const float Cx = -(c.R[0] * c.t[0] + c.R[3] * c.t[1] + c.R[6] * c.t[2]);
+    const float Cy = -(c.R[1] * c.t[0] + c.R[4] * c.t[1] + c.R[7] * c.t[2]);
+    const float Cz = -(c.R[2] * c.t[0] + c.R[5] * c.t[1] + c.R[8] * c.t[2]);
+    out[0] = tx + Cx;
+    out[1] = ty + Cy;
+    out[2] = tz + Cz;
+}
+
+// ProjectonCamera_cu (patch_match_kernel.cu:622-648)
+__device__ __forceinline__ void project_on_camera(const float X[3], const DevCam& c, float& u, float& v,
+                                                  float& depth) {
+    const float tx = c.R[0] * X[0] + c.R[1] * X[1] + c.R[2] * X[2] + c.t[0];
+    const float ty = c.R[3] * X[0] + c.R[4] * X[1] + c.R[5] * X[2] + c.t[1];
+    const float tz = c.R[6] * X[0] + c.R[7] * X[1] + c.R[8] * X[2] + c.t[2];
+    depth = c.K[6] * tx + c.K[7] * ty + c.K[8] * tz;
+    u = (c.K[0] * tx + c.K[1] * ty + c.K[2] * tz) / depth;
+    v = (c.K[3] * tx + c.K[4] * ty + c.K[5] * tz) / depth;
+}
+
+}  // namespace gmvs

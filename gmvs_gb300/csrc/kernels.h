@@ -1,0 +1,51 @@
+// Host-side launchers of the device kernels (internal to the library).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace gmvs {
+
+// Sampler/staging variants of the PatchMatch kernels.
+enum SamplerVariant : int { kVarF32 = 0, kVarQuadF32 = 1, kVarQuadF16 = 2, kVarTex = 3, kNumVariants = 4 };
+
+struct LaunchShape {
+    int grid;      // CTAs (persistent: each loops over tiles)
+    dim3 block;    // (tile width, tile thread rows)
+    size_t smem;   // dynamic shared memory bytes
+};
+
+// One entry per variant, defined in pm_<variant>.cu.
+cudaError_t launch_init_f32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*, int*,
+                            bool generic, cudaStream_t);
+cudaError_t launch_sweep_f32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*, int,
+                             int*, bool generic, cudaStream_t);
+cudaError_t launch_init_qf32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*, int*,
+                             bool generic, cudaStream_t);
+cudaError_t launch_sweep_qf32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*, int,
+                              int*, bool generic, cudaStream_t);
+cudaError_t launch_init_qf16(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*, int*,
+                             bool generic, cudaStream_t);
+cudaError_t launch_sweep_qf16(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*, int,
+                              int*, bool generic, cudaStream_t);
+cudaError_t launch_init_tex(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*, int*,
+                            bool generic, cudaStream_t);
+cudaError_t launch_sweep_tex(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*, int, int*,
+                             bool generic, cudaStream_t);
+// Per-pixel NCC cost matrix of given hypotheses (gmvs_ncc_costs).
+cudaError_t launch_ncc_f32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*,
+                           const float4*, float*, float*, uint32_t*, bool generic, cudaStream_t);
+cudaError_t launch_ncc_qf32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*,
+                            const float4*, float*, float*, uint32_t*, bool generic, cudaStream_t);
+cudaError_t launch_ncc_qf16(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*,
+                            const float4*, float*, float*, uint32_t*, bool generic, cudaStream_t);
+cudaError_t launch_ncc_tex(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*,
+                           const float4*, float*, float*, uint32_t*, bool generic, cudaStream_t);
+
+// Finalisation (runtime.cu): conversion, filter + export of one colour.
+cudaError_t launch_convert(const LaunchShape&, const DevView*, const Tile*, const int*, int final_buf, cudaStream_t);
+cudaError_t launch_filter(const LaunchShape&, const DevView*, const Tile*, const int*, int final_buf, int colour,
+                          int run_filter, cudaStream_t);
+
+}  // namespace gmvs

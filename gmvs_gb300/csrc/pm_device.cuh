@@ -1,0 +1,999 @@
+// PatchMatch device code: samplers, the reference-side patch, the bilateral
+// NCC, initialisation, one checkerboard half-sweep (propagation + joint view
+// selection + refinement), depth/normal conversion and the median filter.
+// Included by one .cu file per sampler so the instantiations compile in
+// parallel.
+#pragma once
+
+#include "common.cuh"
+
+namespace gmvs {
+
+// --------------------------------------------------------------- samplers --
+// All samplers reproduce module B's truncate-then-clamp bilinear
+// (gmvs/src/patch_match.cu:10-33) except SampTex, which is module A's
+// hardware tex2D (patch_match_kernel.cu:443-464).
+struct SampF32 {  // plain fp32 rows, four loads per sample
+    const float* __restrict__ p;
+    int H, W;
+    __device__ __forceinline__ SampF32(const DevView& V, int img) : p((const float*)V.img[img]), H(V.H), W(V.W) {}
+    __device__ __forceinline__ float at(int x, int y) const { return __ldg(p + y * W + x); }
+    __device__ __forceinline__ float sample(float u, float v) const { return bilinear_clamp(p, u, v, H, W); }
+    static constexpr bool kTex = false;
+};
+
+// Texel quads: quad[y][x] = (I[y][x], I[y][xu], I[yu][x], I[yu][xu]) with
+// xu = min(x+1, W-1), yu = min(y+1, H-1), i.e. the four taps the reference
+// reads for a sample whose clamped integer corner is (x, y).
+__device__ __forceinline__ void clamp_corner(float u, float v, int H, int W, int& idx, float& wd, float& hd) {
+    const int hl = min(max(__float2int_rz(v), 0), H - 1);
+    const int wl = min(max(__float2int_rz(u), 0), W - 1);
+    hd = v - (float)hl;
+    wd = u - (float)wl;
+    idx = hl * W + wl;
+}
+
+struct SampQuadF32 {
+    const float4* __restrict__ p;
+    int H, W;
+    __device__ __forceinline__ SampQuadF32(const DevView& V, int img)
+        : p((const float4*)V.img[img]), H(V.H), W(V.W) {}
+    __device__ __forceinline__ float at(int x, int y) const { return __ldg(&p[y * W + x]).x; }
+    __device__ __forceinline__ float sample(float u, float v) const {
+        int idx;
+        float wd, hd;
+        clamp_corner(u, v, H, W, idx, wd, hd);
+        const float4 q = __ldg(&p[idx]);
+        return lerpf(lerpf(q.x, q.y, wd), lerpf(q.z, q.w, wd), hd);
+    }
+    static constexpr bool kTex = false;
+};
+
+struct SampQuadF16 {
+    const uint2* __restrict__ p;
+    int H, W;
+    __device__ __forceinline__ SampQuadF16(const DevView& V, int img)
+        : p((const uint2*)V.img[img]), H(V.H), W(V.W) {}
+    __device__ __forceinline__ static float2 h2f(uint32_t u) {
+        __half2 h = *reinterpret_cast<__half2*>(&u);
+        return __half22float2(h);
+    }
+    __device__ __forceinline__ float at(int x, int y) const { return h2f(__ldg(&p[y * W + x]).x).x; }
+    __device__ __forceinline__ float sample(float u, float v) const {
+        int idx;
+        float wd, hd;
+        clamp_corner(u, v, H, W, idx, wd, hd);
+        const uint2 q = __ldg(&p[idx]);
+        const float2 t = h2f(q.x), b = h2f(q.y);
+        return lerpf(lerpf(t.x, t.y, wd), lerpf(b.x, b.y, wd), hd);
+    }
+    static constexpr bool kTex = false;
+};
+
+struct SampTex {
+    cudaTextureObject_t t;
+    __device__ __forceinline__ SampTex(const DevView& V, int img) : t((cudaTextureObject_t)V.tex[img]) {}
+    __device__ __forceinline__ float at(int x, int y) const {
+        return tex2D<float>(t, (float)x + 0.5f, (float)y + 0.5f);
+    }
+    __device__ __forceinline__ float sample(float u, float v) const { return tex2D<float>(t, u + 0.5f, v + 0.5f); }
+    static constexpr bool kTex = true;
+};
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// -------------------------------------------------------- reference patch --
+// The bilateral weights, the reference samples and the reference moments do
+// not depend on the hypothesis (ComputeBilateralWeight depends only on the
+// window offset and |I_ref - I_ref(centre)|, patch_match_kernel.cu:397-410),
+// so they are formed once per pixel per launch.  NS = samples per axis
+// (6 for the default 11x11 window with stride 2); NS = 0 is the generic path
+// that recomputes them per sample for other window shapes.
+template <int NS>
+struct Patch {
+    float w[NS * NS];
+    float wr[NS * NS];
+    float qx[NS];
+    float qy[NS];
+    float inv, mean_r, var_r;
+};
+template <>
+struct Patch<0> {
+    float center, inv, mean_r, var_r;
+};
+
+__device__ __forceinline__ float bilateral_weight(float xd, float yd, float pix, float center, float ss, float sc) {
+    const float sd = sqrtf(xd * xd + yd * yd);
+    const float cd = fabsf(pix - center);
+    return expf(-sd / (2.0f * ss * ss) - cd / (2.0f * sc * sc));
+}
+
+template <class S, int NS>
+__device__ __forceinline__ void make_patch(Patch<NS>& P, const S& ref, const DevView& V, const DevParams& prm, int px,
+                                           int py) {
+    const int radius = prm.patch_size / 2;
+    const int inc = prm.radius_increment;
+    float s_w = 0.f, s_r = 0.f, s_rr = 0.f;
+    if constexpr (NS > 0) {
+        const float center = ref.at(px, py);
+#pragma unroll
+        for (int a = 0; a < NS; ++a) {
+            const int off = -radius + a * inc;
+            if constexpr (S::kTex) {
+                P.qx[a] = (float)(px + off);
+                P.qy[a] = (float)(py + off);
+            } else {
+                P.qx[a] = (float)min(max(px + off, 0), V.W - 1);
+                P.qy[a] = (float)min(max(py + off, 0), V.H - 1);
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < NS; ++a) {
+            float c_w = 0.f, c_r = 0.f, c_rr = 0.f;
+#pragma unroll
+            for (int b = 0; b < NS; ++b) {
+                const float r = ref.at((int)P.qx[a], (int)P.qy[b]);
+                const float w = bilateral_weight((float)(-radius + a * inc), (float)(-radius + b * inc), r, center,
+                                                 prm.sigma_spatial, prm.sigma_color);
+                const float wr = w * r;
+                P.w[a * NS + b] = w;
+                P.wr[a * NS + b] = wr;
+                if constexpr (S::kTex) {  // module A sums per window column
+                    c_r += wr;
+                    c_rr += wr * r;
+                    c_w += w;
+                } else {
+                    s_r += wr;
+                    s_rr += wr * r;
+                    s_w += w;
+                }
+            }
+            if constexpr (S::kTex) {
+                s_r += c_r;
+                s_rr += c_rr;
+                s_w += c_w;
+            }
+        }
+    } else {
+        P.center = ref.at(px, py);
+        for (int i = -radius; i < radius + 1; i += inc) {
+            float c_w = 0.f, c_r = 0.f, c_rr = 0.f;
+            for (int j = -radius; j < radius + 1; j += inc) {
+                int qx = px + i, qy = py + j;
+                if constexpr (!S::kTex) {
+                    qx = min(max(qx, 0), V.W - 1);
+                    qy = min(max(qy, 0), V.H - 1);
+                }
+                const float r = ref.at(qx, qy);
+                const float w =
+                    bilateral_weight((float)i, (float)j, r, P.center, prm.sigma_spatial, prm.sigma_color);
+                c_r += w * r;
+                c_rr += w * r * r;
+                c_w += w;
+            }
+            s_r += c_r;
+            s_rr += c_rr;
+            s_w += c_w;
+        }
+    }
+    P.inv = 1.0f / s_w;
+    P.mean_r = s_r * P.inv;
+    P.var_r = s_rr * P.inv - P.mean_r * P.mean_r;
+}
+
+// Hypothesis-dependent row of the homography: g = K_r^-T n / w.
+struct Hyp {
+    float g0, g1, g2;
+};
+__device__ __forceinline__ Hyp make_hyp(const DevCam& rc, float4 pl) {
+    const float fx = rc.K[0], fy = rc.K[4], cx = rc.K[2], cy = rc.K[5];
+    const float iw = 1.0f / pl.w;
+    Hyp h;
+    h.g0 = pl.x / fx * iw;
+    h.g1 = pl.y / fy * iw;
+    h.g2 = (pl.z - pl.x * cx / fx - pl.y * cy / fy) * iw;
+    return h;
+}
+
+// Bilateral NCC of one hypothesis against source j (0-based): ComputeBilateralNCC
+// (patch_match_kernel.cu:412-516; gmvs/src/patch_match.cu:347-445).
+template <class S, int NS>
+__device__ __forceinline__ float ncc_cost(const DevView& V, const DevParams& prm, int j, const Hyp& h,
+                                          const Patch<NS>& P, int px, int py) {
+    const float* A = V.A[j];
+    const float* b = V.b[j];
+    const float m0 = fmaf(-b[0], h.g0, A[0]), m1 = fmaf(-b[0], h.g1, A[1]), m2 = fmaf(-b[0], h.g2, A[2]);
+    const float m3 = fmaf(-b[1], h.g0, A[3]), m4 = fmaf(-b[1], h.g1, A[4]), m5 = fmaf(-b[1], h.g2, A[5]);
+    const float m6 = fmaf(-b[2], h.g0, A[6]), m7 = fmaf(-b[2], h.g1, A[7]), m8 = fmaf(-b[2], h.g2, A[8]);
+    const float fpx = (float)px, fpy = (float)py;
+    const float cz = m6 * fpx + m7 * fpy + m8;
+    const float cu = (m0 * fpx + m1 * fpy + m2) / cz;
+    const float cv = (m3 * fpx + m4 * fpy + m5) / cz;
+    if (cu >= V.src_w[j] || cu < 0.0f || cv >= V.src_h[j] || cv < 0.0f) return 2.0f;
+    const S src(V, j + 1);
+    float ss = 0.f, sss = 0.f, srs = 0.f;
+    if constexpr (NS > 0) {
+#pragma unroll
+        for (int a = 0; a < NS; ++a) {
+            const float qx = P.qx[a];
+            const float bx = fmaf(m0, qx, m2), by = fmaf(m3, qx, m5), bz = fmaf(m6, qx, m8);
+#pragma unroll
+            for (int bb = 0; bb < NS; ++bb) {
+                const float qy = P.qy[bb];
+                const float Z = fmaf(m7, qy, bz);
+                const float rz = rcp_approx(Z);
+                const float u = fmaf(m1, qy, bx) * rz;
+                const float v = fmaf(m4, qy, by) * rz;
+                const float s = src.sample(u, v);
+                const float ws = P.w[a * NS + bb] * s;
+                ss += ws;
+                sss = fmaf(ws, s, sss);
+                srs = fmaf(P.wr[a * NS + bb], s, srs);
+            }
+        }
+    } else {
+        const int radius = prm.patch_size / 2;
+        const int inc = prm.radius_increment;
+        const S ref(V, 0);
+        for (int i = -radius; i < radius + 1; i += inc) {
+            for (int jj = -radius; jj < radius + 1; jj += inc) {
+                int qx = px + i, qy = py + jj;
+                if constexpr (!S::kTex) {
+                    qx = min(max(qx, 0), V.W - 1);
+                    qy = min(max(qy, 0), V.H - 1);
+                }
+                const float r = ref.at(qx, qy);
+                const float w =
+                    bilateral_weight((float)i, (float)jj, r, P.center, prm.sigma_spatial, prm.sigma_color);
+                const float fqx = (float)qx, fqy = (float)qy;
+                const float Z = m6 * fqx + m7 * fqy + m8;
+                const float rz = rcp_approx(Z);
+                const float u = (m0 * fqx + m1 * fqy + m2) * rz;
+                const float v = (m3 * fqx + m4 * fqy + m5) * rz;
+                const float s = src.sample(u, v);
+                const float ws = w * s;
+                ss += ws;
+                sss = fmaf(ws, s, sss);
+                srs = fmaf(w * r, s, srs);
+            }
+        }
+    }
+    const float sm = ss * P.inv;
+    const float sq = sss * P.inv;
+    const float sr = srs * P.inv;
+    const float var_s = sq - sm * sm;
+    if (P.var_r < 1e-5f || var_s < 1e-5f) return 2.0f;
+    const float cov = sr - P.mean_r * sm;
+    const float vrs = sqrtf(P.var_r * var_s);
+    return fmaxf(0.0f, fminf(2.0f, 1.0f - cov / vrs));
+}
+
+// ----------------------------------------------------------- camera math --
+__device__ __forceinline__ float depth_from_plane(const DevCam& c, float4 pl, int px, int py) {
+    return -pl.w * c.K[0] /
+           (((float)px - c.K[2]) * pl.x + (c.K[0] / c.K[4]) * ((float)py - c.K[5]) * pl.y + c.K[0] * pl.z);
+}
+__device__ __forceinline__ void get_3d_point(const DevCam& c, int px, int py, float depth, float X[3]) {
+    X[0] = depth * ((float)px - c.K[2]) / c.K[0];
+    X[1] = depth * ((float)py - c.K[5]) / c.K[4];
+    X[2] = depth;
+}
+__device__ __forceinline__ float distance_to_origin(const DevCam& c, int px, int py, float depth, float4 n) {
+    float X[3];
+    get_3d_point(c, px, py, depth, X);
+    return -(n.x * X[0] + n.y * X[1] + n.z * X[2]);
+}
+__device__ __forceinline__ float4 view_direction(const DevCam& c, int px, int py, float depth) {
+    float X[3];
+    get_3d_point(c, px, py, depth, X);
+    const float norm = sqrtf(X[0] * X[0] + X[1] * X[1] + X[2] * X[2]);
+    return make_float4(X[0] / norm, X[1] / norm, X[2] / norm, 0.0f);
+}
+__device__ __forceinline__ void normalize3(float4& v) {
+    const float inv = 1.0f / sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+    v.x *= inv;
+    v.y *= inv;
+    v.z *= inv;
+}
+__device__ __forceinline__ float4 normal_to_world(const DevCam& c, float4 p) {
+    return make_float4(c.R[0] * p.x + c.R[3] * p.y + c.R[6] * p.z, c.R[1] * p.x + c.R[4] * p.y + c.R[7] * p.z,
+                       c.R[2] * p.x + c.R[5] * p.y + c.R[8] * p.z, p.w);
+}
+__device__ __forceinline__ float4 normal_to_cam(const DevCam& c, float4 p) {
+    return make_float4(c.R[0] * p.x + c.R[1] * p.y + c.R[2] * p.z, c.R[3] * p.x + c.R[4] * p.y + c.R[5] * p.z,
+                       c.R[6] * p.x + c.R[7] * p.y + c.R[8] * p.z, p.w);
+}
+
+// GenerateRandomNormal (patch_match_kernel.cu:137-172); rejection bounded at 64.
+__device__ __forceinline__ float4 random_normal(const DevCam& c, int px, int py, DevRng& rng, float depth) {
+    float q1 = 1.0f, q2 = 1.0f, s = 2.0f;
+    for (int it = 0; it < 64 && s >= 1.0f; ++it) {
+        q1 = 2.0f * rng.uniform() - 1.0f;
+        q2 = 2.0f * rng.uniform() - 1.0f;
+        s = q1 * q1 + q2 * q2;
+    }
+    if (s >= 1.0f) {
+        q1 = 0.0f;
+        q2 = 0.0f;
+        s = 0.0f;
+    }
+    const float sq = sqrtf(1.0f - s);
+    float4 n = make_float4(2.0f * q1 * sq, 2.0f * q2 * sq, 1.0f - 2.0f * s, 0.0f);
+    const float4 vd = view_direction(c, px, py, depth);
+    if (n.x * vd.x + n.y * vd.y + n.z * vd.z > 0.0f) {
+        n.x = -n.x;
+        n.y = -n.y;
+        n.z = -n.z;
+    }
+    normalize3(n);
+    return n;
+}
+
+// GeneratePerturbedNormal (patch_match_kernel.cu:174-213)
+__device__ __forceinline__ float4 perturbed_normal(const DevCam& c, int px, int py, float4 n, DevRng& rng, float pert) {
+    const float4 vd = view_direction(c, px, py, 1.0f);
+    const float a1 = (rng.uniform() - 0.5f) * pert;
+    const float a2 = (rng.uniform() - 0.5f) * pert;
+    const float a3 = (rng.uniform() - 0.5f) * pert;
+    const float s1 = sinf(a1), s2 = sinf(a2), s3 = sinf(a3);
+    const float c1 = cosf(a1), c2 = cosf(a2), c3 = cosf(a3);
+    const float R0 = c2 * c3, R1 = c3 * s1 * s2 - c1 * s3, R2 = s1 * s3 + c1 * c3 * s2;
+    const float R3 = c2 * s3, R4 = c1 * c3 + s1 * s2 * s3, R5 = c1 * s2 * s3 - c3 * s1;
+    const float R6 = -s2, R7 = c2 * s1, R8 = c1 * c2;
+    float4 np = make_float4(R0 * n.x + R1 * n.y + R2 * n.z, R3 * n.x + R4 * n.y + R5 * n.z,
+                            R6 * n.x + R7 * n.y + R8 * n.z, 0.0f);
+    if (np.x * vd.x + np.y * vd.y + np.z * vd.z >= 0.0f) np = n;
+    normalize3(np);
+    return np;
+}
+
+// compute_geom_consistency_cost (gmvs/src/patch_match.cu:562-593)
+__device__ __forceinline__ float geom_cost(const DevView& V, int j, float4 pl, int px, int py) {
+    const DevCam& rc = V.cam[0];
+    const DevCam& sc = V.cam[j + 1];
+    const float depth = depth_from_plane(rc, pl, px, py);
+    float X[3];
+    point_on_world((float)px, (float)py, depth, rc, X);
+    float su, sv, sd;
+    project_on_camera(X, sc, su, sv, sd);
+    const float src_depth = bilinear_clamp(V.dep[j + 1], su, sv, V.H, V.W);
+    if (src_depth == 0.0f) return 5.0f;
+    float Y[3];
+    point_on_world(su, sv, src_depth, sc, Y);
+    float bu, bv, bd;
+    project_on_camera(Y, rc, bu, bv, bd);
+    const float dc = (float)px - bu, dr = (float)py - bv;
+    return fminf(5.0f, sqrtf(dc * dc + dr * dr));
+}
+
+// planar-prior restricted cost (patch_match_kernel.cu:1256-1290, 784-801)
+struct PriorK {
+    float gamma, two_dsq, two_asq, beta, depth_sigma, angle_sigma;
+};
+__device__ __forceinline__ PriorK prior_k(const DevView& V) {
+    PriorK k;
+    k.gamma = 0.5f;
+    k.depth_sigma = (V.depth_max - V.depth_min) / 64.0f;
+    k.two_dsq = 2 * k.depth_sigma * k.depth_sigma;
+    k.angle_sigma = (float)(3.14159265358979323846 * (5.0f / 180.0f));
+    k.two_asq = 2 * k.angle_sigma * k.angle_sigma;
+    k.beta = 0.18f;
+    return k;
+}
+__device__ __forceinline__ float restricted(const PriorK& k, float cost, float dd, float ac) {
+    const float ad = acosf(ac);
+    const float pr = k.gamma + expf(-dd * dd / k.two_dsq) * expf(-ad * ad / k.two_asq);
+    return expf(-cost * cost / k.beta) * pr;
+}
+
+// insertion sort, FindMinCostIndex / FindMaxCostIndex (patch_match_kernel.cu:5-37)
+__device__ __forceinline__ int find_min_idx8(const float* c) {
+    float m = c[0];
+    int mi = 0;
+#pragma unroll
+    for (int i = 1; i < 8; ++i)
+        if (c[i] <= m) {
+            m = c[i];
+            mi = i;
+        }
+    return mi;
+}
+__device__ __forceinline__ int find_max_idx8(const float* c) {
+    float m = c[0];
+    int mi = 0;
+#pragma unroll
+    for (int i = 1; i < 8; ++i)
+        if (c[i] >= m) {
+            m = c[i];
+            mi = i;
+        }
+    return mi;
+}
+
+// ------------------------------------------------------------------ init --
+// One pixel of RandomInitialization (patch_match_kernel.cu:1467-1577) or of
+// module B's initialization (gmvs/src/patch_match.cu:1046-1082).  `cv` is
+// this thread's shared-memory row (stride nthr), 2 * nmax floats.
+template <class S, int NS>
+__device__ void init_pixel(const DevView& V, const DevParams& prm, int px, int py, float* cv, int nthr) {
+    const int W = V.W, N = V.N;
+    const int c = py * W + px;
+    const DevCam& rc = V.cam[0];
+    DevRng rng(prm.seed_lo, prm.seed_hi, (uint32_t)c, (uint32_t)V.stream_id, phase_of(prm.pass_index, 0));
+    float4 pl;
+    if (prm.init_kind == GMVS_INIT_DEPTH_NORMAL) {
+        // compute_plane_hypothesis_from_normal_depth (gmvs/src/patch_match.cu:329-339)
+        pl = make_float4(V.ref_normal[c * 3 + 0], V.ref_normal[c * 3 + 1], V.ref_normal[c * 3 + 2], V.dep[0][c]);
+        pl = normal_to_cam(rc, pl);
+        const float depth = pl.w;
+        pl.w = distance_to_origin(rc, px, py, depth, pl);
+    } else if (prm.init_kind == GMVS_INIT_PRIOR) {
+        if (V.prior_masks[c] > 0 && V.init_costs[c] >= 0.1f) {
+            const float pert = 0.02f;
+            const float4 pp = V.prior_planes[c];
+            float d = pp.w;
+            const float dmin = (1 - 3 * pert) * d;
+            const float dmax = (1 + 3 * pert) * d;
+            d = rng.uniform() * (dmax - dmin) + dmin;
+            float4 np = perturbed_normal(rc, px, py, pp, rng, (float)(3 * pert * 3.14159265358979323846));
+            np.w = d;
+            pl = np;
+        } else {
+            pl = V.init_planes[c];
+            const float depth = pl.w;
+            pl.w = distance_to_origin(rc, px, py, depth, pl);
+        }
+    } else {
+        const float depth = rng.uniform() * (V.depth_max - V.depth_min) + V.depth_min;
+        pl = random_normal(rc, px, py, rng, depth);
+        pl.w = distance_to_origin(rc, px, py, depth, pl);
+    }
+    Patch<NS> P;
+    make_patch<S, NS>(P, S(V, 0), V, prm, px, py);
+    const Hyp h = make_hyp(rc, pl);
+    int valid = 0;
+    for (int i = 0; i < N; ++i) {
+        const float v = ncc_cost<S, NS>(V, prm, i, h, P, px, py);
+        cv[i * nthr] = v;
+        cv[(prm.nmax + i) * nthr] = v;
+        if (v < 2.0f) valid++;
+    }
+    // ComputeMultiViewInitialCostandSelectedViews (patch_match_kernel.cu:518-569)
+    float* srt = cv + prm.nmax * nthr;
+    for (int i = 1; i < N; i++) {
+        const float tmp = srt[i * nthr];
+        int j = i;
+        for (; j >= 1 && tmp < srt[(j - 1) * nthr]; j--) srt[j * nthr] = srt[(j - 1) * nthr];
+        srt[j * nthr] = tmp;
+    }
+    uint32_t sel = 0;
+    float cost = 2.0f;
+    const int top_k = min(valid, prm.top_k);
+    if (top_k > 0) {
+        float acc = 0.0f;
+        for (int i = 0; i < top_k; ++i) acc += srt[i * nthr];
+        const float thr = srt[(top_k - 1) * nthr];
+        for (int i = 0; i < N; ++i)
+            if (cv[i * nthr] <= thr) sel |= 1u << i;
+        cost = acc / (float)top_k;
+    }
+    V.plane[0][c] = pl;
+    V.cost[0][c] = cost;
+    V.sel[0][c] = sel;
+}
+
+// --------------------------------------------------------------- sweep --
+// One pixel of a half-sweep: CheckerboardPropagation (patch_match_kernel.cu:
+// 813-1351; gmvs/src/patch_match.cu:678-1041) then PlaneHypothesisRefinement
+// (patch_match_kernel.cu:684-811; gmvs/src/patch_match.cu:595-676).
+// Reads the state at the start of the half-sweep (buffer `same` for this
+// colour, `opp` for the other) and writes the pixel to buffer `outb`.
+// `my` is this thread's shared-memory slot (stride nthr): the 8 x nmax cost
+// matrix followed by nmax view weights.
+template <class S, int NS>
+__device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int py, int iter, int colour, float* my,
+                            int nthr) {
+    const int W = V.W, H = V.H, N = V.N, nmax = prm.nmax;
+    const int center = py * W + px;
+    const int same = iter & 1;
+    const int opp = colour == 0 ? (iter & 1) : ((iter + 1) & 1);
+    const int outb = (iter + 1) & 1;
+    const float* __restrict__ cs = V.cost[same];
+    const float* __restrict__ co = V.cost[opp];
+    const DevCam& rc = V.cam[0];
+    const bool geom = prm.sweep_kind == GMVS_SWEEP_GEOM;
+    const bool prior_mode = prm.sweep_kind == GMVS_SWEEP_PRIOR;
+#define CA(k, i) my[((k) * nmax + (i)) * nthr]
+#define VW(i) my[(8 * nmax + (i)) * nthr]
+
+    DevRng rng(prm.seed_lo, prm.seed_hi, (uint32_t)center, (uint32_t)V.stream_id,
+               phase_of(prm.pass_index, 1 + 2 * iter + colour));
+    Patch<NS> P;
+    make_patch<S, NS>(P, S(V, 0), V, prm, px, py);
+
+    // Adaptive checkerboard sampling.  pos = linear index; the buffer of a
+    // candidate follows from its offset parity (odd = other colour).
+    int pos[8];
+    unsigned flags = 0u, fromsame = 0u;
+    float cmin;
+    int cminp;
+    bool csame;
+    // up_far (odd offsets only)
+    if (py > 2) {
+        flags |= 1u << 1;
+        cminp = center - 3 * W;
+        cmin = co[cminp];
+        for (int i = 1; i < 11; ++i)
+            if (py > 2 + 2 * i) {
+                const int t = center - 3 * W - 2 * i * W;
+                const float v = co[t];
+                if (v < cmin) {
+                    cmin = v;
+                    cminp = t;
+                }
+            }
+        pos[1] = cminp;
+    }
+    if (py < H - 3) {  // down_far
+        flags |= 1u << 3;
+        cminp = center + 3 * W;
+        cmin = co[cminp];
+        for (int i = 1; i < 11; ++i)
+            if (py < H - 3 - 2 * i) {
+                const int t = center + 3 * W + 2 * i * W;
+                const float v = co[t];
+                if (v < cmin) {
+                    cmin = v;
+                    cminp = t;
+                }
+            }
+        pos[3] = cminp;
+    }
+    if (px > 2) {  // left_far
+        flags |= 1u << 5;
+        cminp = center - 3;
+        cmin = co[cminp];
+        for (int i = 1; i < 11; ++i)
+            if (px > 2 + 2 * i) {
+                const int t = center - 3 - 2 * i;
+                const float v = co[t];
+                if (v < cmin) {
+                    cmin = v;
+                    cminp = t;
+                }
+            }
+        pos[5] = cminp;
+    }
+    if (px < W - 3) {  // right_far keeps the maximum (patch_match_kernel.cu:954)
+        flags |= 1u << 7;
+        cminp = center + 3;
+        cmin = co[cminp];
+        for (int i = 1; i < 11; ++i)
+            if (px < W - 3 - 2 * i) {
+                const int t = center + 3 + 2 * i;
+                const float v = co[t];
+                if (cmin < v) {
+                    cmin = v;
+                    cminp = t;
+                }
+            }
+        pos[7] = cminp;
+    }
+    // near neighbours: the first candidate (offset 1) has the other colour,
+    // the V-shaped ones (offset parity even) this colour.
+    if (py > 0) {  // up_near
+        flags |= 1u << 0;
+        cminp = center - W;
+        cmin = co[cminp];
+        csame = false;
+        for (int i = 0; i < 3; ++i) {
+            if (py > 1 + i && px > i) {
+                const int t = center - W - (1 + i) * W - i;
+                const float v = cs[t];
+                if (v < cmin) {
+                    cmin = v;
+                    cminp = t;
+                    csame = true;
+                }
+            }
+            if (py > 1 + i && px < W - 1 - i) {
+                const int t = center - W - (1 + i) * W + i;
+                const float v = cs[t];
+                if (v < cmin) {
+                    cmin = v;
+                    cminp = t;
+                    csame = true;
+                }
+            }
+        }
+        pos[0] = cminp;
+        if (csame) fromsame |= 1u << 0;
+    }
+    if (py < H - 1) {  // down_near
+        flags |= 1u << 2;
+        cminp = center + W;
+        cmin = co[cminp];
+        csame = false;
+        for (int i = 0; i < 3; ++i) {
+            if (py < H - 2 - i && px > i) {
+                const int t = center + W + (1 + i) * W - i;
+                const float v = cs[t];
+                if (v < cmin) {
+                    cmin = v;
+                    cminp = t;
+                    csame = true;
+                }
+            }
+            if (py < H - 2 - i && px < W - 1 - i) {
+                const int t = center + W + (1 + i) * W + i;
+                const float v = cs[t];
+                if (v < cmin) {
+                    cmin = v;
+                    cminp = t;
+                    csame = true;
+                }
+            }
+        }
+        pos[2] = cminp;
+        if (csame) fromsame |= 1u << 2;
+    }
+    if (px > 0) {  // left_near
+        flags |= 1u << 4;
+        cminp = center - 1;
+        cmin = co[cminp];
+        csame = false;
+        for (int i = 0; i < 3; ++i) {
+            if (px > 1 + i && py > i) {
+                const int t = center - 1 - (1 + i) - i * W;
+                const float v = cs[t];
+                if (v < cmin) {
+                    cmin = v;
+                    cminp = t;
+                    csame = true;
+                }
+            }
+            if (px > 1 + i && py < H - 1 - i) {
+                const int t = center - 1 - (1 + i) + i * W;
+                const float v = cs[t];
+                if (v < cmin) {
+                    cmin = v;
+                    cminp = t;
+                    csame = true;
+                }
+            }
+        }
+        pos[4] = cminp;
+        if (csame) fromsame |= 1u << 4;
+    }
+    if (px < W - 1) {  // right_near
+        flags |= 1u << 6;
+        cminp = center + 1;
+        cmin = co[cminp];
+        csame = false;
+        for (int i = 0; i < 3; ++i) {
+            if (px < W - 2 - i && py > i) {
+                const int t = center + 1 + (1 + i) - i * W;
+                const float v = cs[t];
+                if (v < cmin) {
+                    cmin = v;
+                    cminp = t;
+                    csame = true;
+                }
+            }
+            if (px < W - 2 - i && py < H - 1 - i) {
+                const int t = center + 1 + (1 + i) + i * W;
+                const float v = cs[t];
+                if (v < cmin) {
+                    cmin = v;
+                    cminp = t;
+                    csame = true;
+                }
+            }
+        }
+        pos[6] = cminp;
+        if (csame) fromsame |= 1u << 6;
+    }
+
+    // cost matrix; rows of out-of-image neighbours keep the reference's
+    // `float cost_array[8][32] = {2.0f}` contents (2 at [0][0], else 0).
+    float4 npl[8];
+    for (int k = 0; k < 8; ++k) {
+        if (flags & (1u << k)) {
+            const float4* src = V.plane[(fromsame >> k) & 1u ? same : opp];
+            npl[k] = src[pos[k]];
+            const Hyp h = make_hyp(rc, npl[k]);
+            for (int i = 0; i < N; ++i) CA(k, i) = ncc_cost<S, NS>(V, prm, i, h, P, px, py);
+        } else {
+            npl[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int i = 0; i < N; ++i) CA(k, i) = (k == 0 && i == 0) ? 2.0f : 0.0f;
+        }
+    }
+
+    // multi-hypothesis joint view selection (patch_match_kernel.cu:1114-1176)
+    const uint32_t* so = V.sel[opp];
+    const uint32_t nb_sel[4] = {(flags & 1u) ? so[center - W] : 0u, (flags & 4u) ? so[center + W] : 0u,
+                                (flags & 16u) ? so[center - 1] : 0u, (flags & 64u) ? so[center + 1] : 0u};
+    const float thr = prm.cost_thr[iter];
+    const float fallback = expf(thr * thr / (-0.32f));
+    float prob_sum = 0.0f;
+    for (int i = 0; i < N; ++i) {
+        float pri = 0.0f;
+        for (int q = 0; q < 4; ++q)
+            if (flags & (1u << (2 * q))) pri += ((nb_sel[q] >> i) & 1u) ? 0.9f : 0.1f;
+        float count = 0.0f, tmpw = 0.0f;
+        int count_false = 0;
+        for (int k = 0; k < 8; ++k) {
+            const float c = CA(k, i);
+            if (c < thr) {
+                tmpw += expf(c * c / (-0.18f));
+                count++;
+            }
+            if (c > 1.2f) count_false++;
+        }
+        float prob = 0.0f;
+        if (count > 2 && count_false < 3)
+            prob = tmpw / count;
+        else if (count_false < 3)
+            prob = fallback;
+        prob = prob * pri;
+        VW(i) = prob;  // PDF held in the weight slots until the draws
+        prob_sum += prob;
+    }
+    {  // TransformPDFToCDF (patch_match_kernel.cu:70-83) then 15 draws
+        const float inv = 1.0f / prob_sum;
+        float cum = 0.0f;
+        for (int i = 0; i < N; ++i) {
+            cum += VW(i) * inv;
+            VW(i) = cum;
+        }
+    }
+    // 15 draws; hits per view (at most 15) are counted in 4-bit fields
+    unsigned long long cnt4[2] = {0ull, 0ull};
+    for (int s = 0; s < 15; ++s) {
+        const float rp = rng.uniform() - 1.1920928955078125e-07f;  // curand_uniform - FLT_EPSILON
+        for (int v = 0; v < N; ++v)
+            if (VW(v) > rp) {
+                cnt4[v >> 4] += 1ull << ((v & 15) * 4);
+                break;
+            }
+    }
+    uint32_t temp_sel = 0;
+    float weight_norm = 0.0f;
+    for (int i = 0; i < N; ++i) {
+        const float w = (float)((cnt4[i >> 4] >> ((i & 15) * 4)) & 15ull);
+        VW(i) = w;
+        if (w > 0) {
+            temp_sel |= 1u << i;
+            weight_norm += w;
+        }
+    }
+
+    // final costs of the 8 candidates (patch_match_kernel.cu:1178-1211;
+    // gmvs/src/patch_match.cu:920-946)
+    float fc[8];
+    for (int k = 0; k < 8; ++k) {
+        float acc = 0.0f;
+        const bool fk = (flags >> k) & 1u;
+        for (int j = 0; j < N; ++j) {
+            const float w = VW(j);
+            if (w > 0) {
+                if (geom && fk)
+                    acc += w * (CA(k, j) + 0.1f * geom_cost(V, j, npl[k], px, py));
+                else
+                    acc += w * CA(k, j);
+            }
+        }
+        fc[k] = acc / weight_norm;
+    }
+    const int min_idx = find_min_idx8(fc);
+
+    // current hypothesis (views with zero weight add +0 in the reference)
+    float4 cur = V.plane[same][center];
+    float cost_now = 0.0f;
+    {
+        const Hyp h = make_hyp(rc, cur);
+        for (int i = 0; i < N; ++i) {
+            const float w = VW(i);
+            if (w > 0) {
+                const float c = ncc_cost<S, NS>(V, prm, i, h, P, px, py);
+                if (geom)
+                    cost_now += w * (c + 0.1f * geom_cost(V, i, cur, px, py));
+                else
+                    cost_now += w * c;
+            }
+        }
+    }
+    cost_now /= weight_norm;
+    float cur_cost = cost_now;
+    uint32_t cur_sel = V.sel[same][center];
+    float depth_now = depth_from_plane(rc, cur, px, py);
+    float restricted_cost = 0.0f;
+    const PriorK pk = prior_k(V);
+    const uint32_t mask = prior_mode ? V.prior_masks[center] : 0u;
+    float4 ppl = make_float4(0.f, 0.f, 0.f, 0.f);
+    float depth_prior = 0.0f;
+
+    if (prior_mode) {
+        ppl = V.prior_planes[center];
+        depth_prior = depth_from_plane(rc, ppl, px, py);
+        if (mask > 0) {
+            float rfc[8];
+            for (int k = 0; k < 8; ++k) {
+                rfc[k] = 0.0f;
+                if ((flags >> k) & 1u) {
+                    const float4 q = npl[k];
+                    const float dn = depth_from_plane(rc, q, px, py);
+                    const float ac = ppl.x * q.x + ppl.y * q.y + ppl.z * q.z;
+                    rfc[k] = restricted(pk, fc[k], dn - depth_prior, ac);
+                }
+            }
+            const int max_idx = find_max_idx8(rfc);
+            const float dn = depth_from_plane(rc, cur, px, py);
+            const float ac = ppl.x * cur.x + ppl.y * cur.y + ppl.z * cur.z;
+            const float rcn = restricted(pk, cost_now, dn - depth_prior, ac);
+            if ((flags >> max_idx) & 1u) {
+                const float4 q = npl[max_idx];
+                const float db = depth_from_plane(rc, q, px, py);
+                if (db >= V.depth_min && db <= V.depth_max && rfc[max_idx] > rcn) {
+                    depth_now = db;
+                    cur = q;
+                    cur_cost = fc[max_idx];
+                    restricted_cost = rfc[max_idx];
+                    cur_sel = temp_sel;
+                }
+            }
+        } else if ((flags >> min_idx) & 1u) {  // no selected-view update (patch_match_kernel.cu:1306-1318)
+            const float4 q = npl[min_idx];
+            const float db = depth_from_plane(rc, q, px, py);
+            if (db >= V.depth_min && db <= V.depth_max && fc[min_idx] < cost_now) {
+                depth_now = db;
+                cur = q;
+                cur_cost = fc[min_idx];
+            }
+        }
+    } else if ((flags >> min_idx) & 1u) {
+        const float4 q = npl[min_idx];
+        const float db = depth_from_plane(rc, q, px, py);
+        if (db >= V.depth_min && db <= V.depth_max && fc[min_idx] < cost_now) {
+            depth_now = db;
+            cur = q;
+            cur_cost = fc[min_idx];
+            cur_sel = temp_sel;
+        }
+    }
+
+    // PlaneHypothesisRefinement (patch_match_kernel.cu:684-811)
+    {
+        const float pert = 0.02f;
+        const bool use_prior = prior_mode && mask > 0;
+        float depth_rand;
+        float4 n_rand;
+        if (use_prior) {
+            depth_rand = rng.uniform() * 6 * pk.depth_sigma + (depth_prior - 3 * pk.depth_sigma);
+            n_rand = perturbed_normal(rc, px, py, ppl, rng, pk.angle_sigma);
+        } else {
+            depth_rand = rng.uniform() * (V.depth_max - V.depth_min) + V.depth_min;
+            n_rand = random_normal(rc, px, py, rng, depth_now);
+        }
+        const float dmin_p = (1 - pert) * depth_now;
+        const float dmax_p = (1 + pert) * depth_now;
+        const float depth_pert = rng.uniform() * (dmax_p - dmin_p) + dmin_p;
+        const float4 n_pert = perturbed_normal(rc, px, py, cur, rng, (float)(pert * 3.14159265358979323846));
+        const float4 base = cur;
+        const float dnow = depth_now;
+        for (int k = 0; k < 5; ++k) {
+            float4 cand;
+            float dk;
+            switch (k) {
+                case 0: cand = base; dk = depth_rand; break;
+                case 1: cand = n_rand; dk = dnow; break;
+                case 2: cand = n_rand; dk = depth_rand; break;
+                case 3: cand = n_pert; dk = dnow; break;
+                default: cand = base; dk = depth_pert; break;
+            }
+            cand.w = distance_to_origin(rc, px, py, dk, cand);
+            const Hyp h = make_hyp(rc, cand);
+            float tc = 0.0f;
+            for (int j = 0; j < N; ++j) {
+                const float w = VW(j);
+                if (w > 0) {
+                    const float c = ncc_cost<S, NS>(V, prm, j, h, P, px, py);
+                    if (geom)
+                        tc += w * (c + 0.1f * geom_cost(V, j, cand, px, py));
+                    else
+                        tc += w * c;
+                }
+            }
+            tc /= weight_norm;
+            const float db = depth_from_plane(rc, cand, px, py);
+            if (use_prior) {
+                const float ac = ppl.x * cand.x + ppl.y * cand.y + ppl.z * cand.z;
+                const float rtc = restricted(pk, tc, dk - depth_prior, ac);
+                if (db >= V.depth_min && db <= V.depth_max && rtc > restricted_cost) {
+                    depth_now = db;
+                    cur = cand;
+                    cur_cost = tc;
+                    restricted_cost = rtc;
+                }
+            } else if (db >= V.depth_min && db <= V.depth_max && tc < cur_cost) {
+                depth_now = db;
+                cur = cand;
+                cur_cost = tc;
+            }
+        }
+    }
+    V.plane[outb][center] = cur;
+    V.cost[outb][center] = cur_cost;
+    V.sel[outb][center] = cur_sel;
+#undef CA
+#undef VW
+}
+
+// ---------------------------------------------------------- finalisation --
+// GetDepthandNormal (patch_match_kernel.cu:1655-1674): depth first, then the
+// normal is rotated to the world frame.
+__device__ __forceinline__ void convert_pixel(const DevView& V, int final_buf, int px, int py) {
+    const int c = py * V.W + px;
+    float4 p = V.plane[final_buf][c];
+    p.w = depth_from_plane(V.cam[0], p, px, py);
+    V.fin[c] = normal_to_world(V.cam[0], p);
+}
+
+// CheckerboardFilter (patch_match_kernel.cu:1355-1463) on fin[].w, in place
+// (only the other colour is read), then the export of this pixel
+// (export_plane_hypotheses_cost, gmvs/src/patch_match.cu:1284-1313).
+__device__ __forceinline__ void filter_export_pixel(const DevView& V, int final_buf, bool run_filter, int px, int py) {
+    const int W = V.W, H = V.H;
+    const int center = py * W + px;
+    float4* __restrict__ pl = V.fin;
+    const float cost = V.cost[final_buf][center];
+    float4 me = pl[center];
+    if (run_filter && !(cost < 0.001f)) {
+        float f[21];
+        int n = 0;
+        f[n++] = me.w;
+        const int left = center - 1, leftleft = center - 3, up = center - W, upup = center - 3 * W;
+        const int down = center + W, downdown = center + 3 * W, right = center + 1, rightright = center + 3;
+        if (py > 0) f[n++] = pl[up].w;
+        if (py > 2) f[n++] = pl[upup].w;
+        if (py > 4) f[n++] = pl[upup - W * 2].w;
+        if (py < H - 1) f[n++] = pl[down].w;
+        if (py < H - 3) f[n++] = pl[downdown].w;
+        if (py < H - 5) f[n++] = pl[downdown + W * 2].w;
+        if (px > 0) f[n++] = pl[left].w;
+        if (px > 2) f[n++] = pl[leftleft].w;
+        if (px > 4) f[n++] = pl[leftleft - 2].w;
+        if (px < W - 1) f[n++] = pl[right].w;
+        if (px < W - 3) f[n++] = pl[rightright].w;
+        if (px < W - 5) f[n++] = pl[rightright + 2].w;
+        if (py > 0 && px < W - 2) f[n++] = pl[up + 2].w;
+        if (py < H - 1 && px < W - 2) f[n++] = pl[down + 2].w;
+        if (py > 0 && px > 1) f[n++] = pl[up - 2].w;
+        if (py < H - 1 && px > 1) f[n++] = pl[down - 2].w;
+        if (px > 0 && py > 2) f[n++] = pl[left - W * 2].w;
+        if (px < W - 1 && py > 2) f[n++] = pl[right - W * 2].w;
+        if (px > 0 && py < H - 2) f[n++] = pl[left + W * 2].w;
+        if (px < W - 1 && py < H - 2) f[n++] = pl[right + W * 2].w;
+        for (int i = 1; i < n; i++) {
+            const float tmp = f[i];
+            int j = i;
+            for (; j >= 1 && tmp < f[j - 1]; j--) f[j] = f[j - 1];
+            f[j] = tmp;
+        }
+        const int m = n / 2;
+        me.w = (n % 2 == 0) ? (f[m - 1] + f[m]) / 2 : f[m];
+        pl[center].w = me.w;
+    }
+    V.out_depth[center] = me.w;
+    V.out_normal[center * 3 + 0] = me.x;
+    V.out_normal[center * 3 + 1] = me.y;
+    V.out_normal[center * 3 + 2] = me.z;
+    V.out_cost[center] = cost;
+    if (V.out_planes) V.out_planes[center] = me;
+}
+
+}  // namespace gmvs

@@ -1,0 +1,247 @@
+/*
+ * gmvs_gb300 — C ABI of the GB300-native ACMP-style PatchMatch MVS hot path.
+ *
+ * Every entry point takes plain pointers and sizes, returns an int32 status
+ * (GMVS_OK == 0) and never throws.  Device pointers are CUDA device
+ * addresses on the current device; `stream` is a cudaStream_t passed as
+ * void* (NULL = legacy default stream).  gmvs_last_error() returns the
+ * message of the last failing call on the calling thread.
+ *
+ * The structs below are layout-compatible with the reference's PODs so the
+ * Python mirrors of `gmvs.src` and `gmvs.lib.build.planar_initer` can fill
+ * them field by field.
+ */
+#ifndef GMVS_GB300_H
+#define GMVS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define GMVS_API __attribute__((visibility("default")))
+#else
+#define GMVS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GMVS_MAX_NGB 32
+#define GMVS_OK 0
+#define GMVS_ERR_INVALID 1    /* bad argument (size, pointer, enum) */
+#define GMVS_ERR_CUDA 2       /* a CUDA runtime call failed */
+#define GMVS_ERR_WORKSPACE 3  /* workspace / scratch too small */
+#define GMVS_ERR_DEVICE 4     /* a kernel reported an error status */
+
+/* Pinhole camera, world->camera X_c = R X_w + t.
+ * Same layout as mvs::Camera (gmvs/include/data_structure.hpp:39-47) and
+ * Camera (gmvs/lib/include/planar_initer.hpp:39-47). 100 bytes. */
+typedef struct gmvs_camera {
+    float K[9];
+    float R[9];
+    float t[3];
+    int32_t height;
+    int32_t width;
+    float depth_min;
+    float depth_max;
+} gmvs_camera;
+
+/* One reference view and its source views.
+ * Same layout as mvs::Problem (gmvs/include/data_structure.hpp:33-37). */
+typedef struct gmvs_problem {
+    int32_t num_ngb;
+    int32_t ref_image_id;
+    int32_t src_image_ids[GMVS_MAX_NGB];
+} gmvs_problem;
+
+/* How the hypothesis field is initialised before the sweeps. */
+enum gmvs_init_kind {
+    GMVS_INIT_RANDOM = 0,       /* RandomInitialization random branch (patch_match_kernel.cu:1560-1576) */
+    GMVS_INIT_PRIOR = 1,        /* planar-prior branch (patch_match_kernel.cu:1513-1559) */
+    GMVS_INIT_DEPTH_NORMAL = 2  /* module B initialization (gmvs/src/patch_match.cu:1046-1082) */
+};
+
+/* Which cost the checkerboard sweeps minimise. */
+enum gmvs_sweep_kind {
+    GMVS_SWEEP_PHOTO = 0,  /* module A, photometric only (patch_match_kernel.cu:813-1351, geom off) */
+    GMVS_SWEEP_PRIOR = 1,  /* module A with the planar-prior restricted cost (patch_match_kernel.cu:1245-1319) */
+    GMVS_SWEEP_GEOM = 2    /* module B, photometric + 0.1*geometric (gmvs/src/patch_match.cu:678-1041) */
+};
+
+/* How source images are sampled.
+ *  TEX: hardware texture, linear filter, unnormalised coordinates at +0.5
+ *       (module A, planar_initer.cu:150-158, patch_match_kernel.cu:443-464);
+ *  CLAMP: fp32 bilinear with the reference's truncate-then-clamp indexing
+ *       (module B, gmvs/src/patch_match.cu:10-33). */
+enum gmvs_sampler { GMVS_SAMPLER_CLAMP = 0, GMVS_SAMPLER_TEX = 1 };
+
+/* Device staging of the images for the CLAMP sampler. */
+enum gmvs_staging {
+    GMVS_STAGE_F32 = 0,       /* plain fp32 rows, four scalar loads per sample */
+    GMVS_STAGE_QUAD_F32 = 1,  /* fp32 texel quads, one 16-byte load per sample */
+    GMVS_STAGE_QUAD_F16 = 2,  /* fp16 texel quads, one 8-byte load per sample */
+    GMVS_STAGE_AUTO = 3       /* library picks (quad f16 when lossless, else quad f32) */
+};
+
+/* PatchMatch parameters: the 17 fields of PatchMatchParams
+ * (gmvs/lib/include/planar_initer.hpp:13-31) in order, then extensions that
+ * default to reference behaviour. */
+typedef struct gmvs_params {
+    int32_t max_iterations;   /* 3 */
+    int32_t patch_size;       /* 11 */
+    int32_t num_images;       /* 5 (set per view from num_src + 1) */
+    int32_t max_image_size;   /* 3200 (unused, as in the reference) */
+    int32_t radius_increment; /* 2 */
+    float sigma_spatial;      /* 5 */
+    float sigma_color;        /* 3 */
+    int32_t top_k;            /* 4 */
+    float baseline;           /* 0.54 (unused) */
+    float depth_min;          /* per-view values come from gmvs_view_pass */
+    float depth_max;
+    float disparity_min;      /* unused */
+    float disparity_max;      /* unused */
+    int32_t geom_consistency;
+    int32_t multi_geometry;   /* unused */
+    int32_t planar_prior;
+    int32_t superpixel_filter;
+    /* extensions */
+    uint64_t seed;            /* Philox key, default 3407 (RANDOM_SEED, patch_match_kernel.cu:3) */
+    int32_t init_kind;        /* gmvs_init_kind */
+    int32_t sweep_kind;       /* gmvs_sweep_kind */
+    int32_t sampler;          /* gmvs_sampler */
+    int32_t staging;          /* gmvs_staging */
+    int32_t pass_index;       /* decorrelates the Philox streams of successive passes */
+    int32_t tile_w;           /* sweep tile width in pixels (0 = 32) */
+    int32_t tile_h;           /* sweep tile height in thread rows (0 = 4) */
+    int32_t run_filter;       /* 1 = depth/normal conversion + checkerboard median filter */
+} gmvs_params;
+
+/* One reference view of one pass.  All pointers are device pointers except
+ * `cams`, which is a host array copied by value.  Views in one call may have
+ * different sizes and source counts. */
+typedef struct gmvs_view_pass {
+    int32_t height;
+    int32_t width;
+    int32_t num_src;                             /* N <= GMVS_MAX_NGB */
+    int32_t stream_id;                           /* Philox stream (reference image id) */
+    float depth_min;                             /* search range of this view */
+    float depth_max;
+    gmvs_camera cams[1 + GMVS_MAX_NGB];          /* ref, then src */
+    const float* images[1 + GMVS_MAX_NGB];       /* fp32 [H][W] gray images (row pitch = width) */
+    const float* depths[1 + GMVS_MAX_NGB];       /* GEOM: input depths [H][W] (ref, then src) */
+    const float* ref_normal;                     /* DEPTH_NORMAL init: world normals [H][W][3] */
+    const float* prior_planes;                   /* PRIOR: float4 [H][W] (camera-frame n, d) */
+    const uint32_t* prior_masks;                 /* PRIOR: [H][W] triangle id + 1, 0 = none */
+    const float* init_planes;                    /* PRIOR init: previous pass planes float4 [H][W] */
+    const float* init_costs;                     /* PRIOR init: previous pass costs [H][W] */
+    float* out_depth;                            /* [H][W] */
+    float* out_normal;                           /* [H][W][3] world frame */
+    float* out_cost;                             /* [H][W] */
+    float* out_planes;                           /* optional float4 [H][W]: exported plane field */
+} gmvs_view_pass;
+
+/* Fusion of one reference view (gmvs/src/fusion.cu:61-182, 211-275). */
+typedef struct gmvs_fuse_view {
+    int32_t height;
+    int32_t width;
+    int32_t num_views;                           /* V, extent of `masks` */
+    gmvs_problem problem;
+    gmvs_camera cams[1 + GMVS_MAX_NGB];          /* ref, then src in problem order */
+    const float* depths[1 + GMVS_MAX_NGB];       /* device [H][W] (ref, then src) */
+    const float* normals[1 + GMVS_MAX_NGB];      /* device [H][W][3] */
+    uint8_t* masks;                              /* device bool [V][H][W], read and written */
+    int32_t geom_consistent;
+    float* out_depth;                            /* device [H][W], zero-filled by the call */
+    float* out_normal;                           /* device [H][W][3], zero-filled by the call */
+    int32_t* out_count;                          /* optional device [H][W]: consistent-view count, -1 = skipped */
+} gmvs_fuse_view;
+
+GMVS_API int32_t gmvs_version(void);
+GMVS_API const char* gmvs_last_error(void);
+
+/* Fill `p` with the reference defaults (PatchMatchParams(), data_structure.hpp:20-37). */
+GMVS_API void gmvs_default_params(gmvs_params* p);
+
+/* ---------------------------------------------------------------- passes --
+ * A plan owns one PatchMatch pass over `n_views` reference views (one view =
+ * the plain per-view path of PlanarInit::run_patch_match,
+ * patch_match_kernel.cu:1711-1809, and PatchMatcher::run_patch_match,
+ * gmvs/src/patch_match.cu:1353-1518; many views = one launch per stage for
+ * the whole batch).  The caller provides the device workspace; the library
+ * allocates no device memory.  Creating a plan uploads descriptors and
+ * stages images on `stream`; gmvs_plan_launch only enqueues kernels (it can
+ * be captured into a CUDA graph). */
+typedef struct gmvs_plan gmvs_plan;
+
+GMVS_API size_t gmvs_plan_workspace_bytes(const gmvs_view_pass* views, int32_t n_views,
+                                 const gmvs_params* params);
+GMVS_API int32_t gmvs_plan_create(const gmvs_view_pass* views, int32_t n_views,
+                         const gmvs_params* params, void* workspace,
+                         size_t workspace_bytes, void* stream, gmvs_plan** out);
+/* Enqueue the whole chain: init, 2*max_iterations half-sweeps, filter, export. */
+GMVS_API int32_t gmvs_plan_launch(gmvs_plan* plan, void* stream);
+/* Number of stages and one stage at a time (for schedulers interleaving plans). */
+GMVS_API int32_t gmvs_plan_num_stages(const gmvs_plan* plan);
+GMVS_API int32_t gmvs_plan_launch_stage(gmvs_plan* plan, int32_t stage, void* stream);
+/* Device error word of the plan's kernels (0 = ok); synchronises `stream`. */
+GMVS_API int32_t gmvs_plan_check(gmvs_plan* plan, void* stream);
+GMVS_API void gmvs_plan_destroy(gmvs_plan* plan);
+
+/* Convenience: create, launch, check and destroy in one call. */
+GMVS_API int32_t gmvs_run_passes(const gmvs_view_pass* views, int32_t n_views,
+                        const gmvs_params* params, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
+/* Per-view NCC costs of given hypotheses: for every pixel of view 0 of
+ * `view`, the bilateral NCC against each source view for the camera-frame
+ * plane planes[y][x] (float4 n, d).  costs: device [num_src][H][W].
+ * Also writes the initial multi-view cost and selected-view mask
+ * (ComputeMultiViewInitialCostandSelectedViews, patch_match_kernel.cu:518-569)
+ * into init_cost / init_views when those are non-NULL. */
+GMVS_API size_t gmvs_ncc_workspace_bytes(const gmvs_view_pass* view, const gmvs_params* params);
+GMVS_API int32_t gmvs_ncc_costs(const gmvs_view_pass* view, const gmvs_params* params,
+                       const float* planes, float* costs, float* init_cost,
+                       uint32_t* init_views, void* workspace, size_t workspace_bytes,
+                       void* stream);
+
+/* ---------------------------------------------------------------- fusion --
+ * Deterministic geometric-consistency fusion of one reference view.  Output
+ * pixels hit by several reference pixels take the value of the highest
+ * reference pixel index (the last writer of a sequential scan). */
+GMVS_API size_t gmvs_fuse_scratch_bytes(int32_t height, int32_t width);
+GMVS_API int32_t gmvs_fuse(const gmvs_fuse_view* args, void* scratch, size_t scratch_bytes,
+                  void* stream);
+
+/* -------------------------------------------------- host (CPU) routines --
+ * Planar prior from a depth/cost map: support points, Delaunay
+ * triangulation, superpixel filter, rasterisation and plane fit
+ * (PlanarInit::triangulation, planar_initer.cu:225-420, 700-745).
+ * out_planes: host float4 [H][W]; out_masks: host uint32 [H][W];
+ * out_tri_count receives the number of retained triangles. */
+GMVS_API int32_t gmvs_build_planar_prior(const gmvs_camera* ref_cam, int32_t height, int32_t width,
+                                const float* depth, const float* cost,
+                                const uint8_t* superpixel, int32_t superpixel_filter,
+                                float depth_min, float depth_max,
+                                float* out_planes, uint32_t* out_masks,
+                                int32_t* out_tri_count, int32_t* out_tris, int32_t max_tris);
+
+/* planar_initer.cu:537-632 */
+GMVS_API int32_t gmvs_fusion_planar_mask(const int32_t* seg_ids, const int32_t* planar_mask,
+                                const float* normals, int32_t rows, int32_t cols,
+                                int32_t thresh, float nonplanar_percent,
+                                float cos_sim_thresh, float match_ratio_thresh,
+                                int32_t* out_mask);
+/* planar_initer.cu:634-684 */
+GMVS_API int32_t gmvs_filter_by_var_map(const float* var_map, const int32_t* seg_ids,
+                               int32_t rows, int32_t cols, float var_thresh,
+                               int32_t* out_ids);
+/* planar_initer.cu:471-535 (host loop) */
+GMVS_API int32_t gmvs_sliding_window_normal(const int32_t* planar_region, const float* normals,
+                                   int32_t rows, int32_t cols, int32_t window_size,
+                                   float* out_normals);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GMVS_GB300_H */
