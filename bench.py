@@ -41,6 +41,8 @@ def parse():
     ap.add_argument("--width", type=int, default=1600)
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-view comparison step")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--profile", action="store_true",
+                    help="run the pipeline once (after one warm-up) and exit: the command profiled by ncu")
     return ap.parse_args()
 
 
@@ -188,6 +190,13 @@ def main():
     sc = synthetic.room_scene(0, H=args.height, W=args.width, num_views=args.views, device=dev)
     inputs = scene_inputs_from_synthetic(sc, dev)
     pipe = ScenePipeline(inputs, mode="batched", prior_threads=min(16, os.cpu_count() or 1))
+    if args.profile:
+        pipe.run()
+        torch.cuda.synchronize()
+        pipe.run()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_run": "ok", "views": args.views, "height": args.height, "width": args.width}))
+        return
     for _ in range(args.warmup):
         pipe.run()
     torch.cuda.synchronize()

@@ -346,7 +346,10 @@ inline T bilinear_clamp(const float* img, T u, T v, int H, int W) {
 // Module A tex2D<float>(tex, x, y) on a float32 texture with
 // cudaFilterModeLinear, unnormalised coordinates (planar_initer.cu:150-158):
 // x_B = x - 0.5, i = floor(x_B), alpha = frac(x_B) held with 8 fractional
-// bits; out-of-range texel indices are clamped to the edge.
+// bits, rounded half up; out-of-range texel indices are clamped to the edge
+// (cudaAddressModeWrap acts as clamp with unnormalised coordinates).  Pinned
+// on a GB300 against 2600 hardware fetches (fraction sweeps in x and y,
+// ties, out-of-range coordinates): all equal bit for bit.
 template <class T>
 inline T tex2d_linear(const float* img, float x, float y, int H, int W) {
     const float xb = x - 0.5f, yb = y - 0.5f;
@@ -357,8 +360,8 @@ inline T tex2d_linear(const float* img, float x, float y, int H, int W) {
         a = (T)xb - (T)fx;
         b = (T)yb - (T)fy;
     } else {
-        a = (T)(std::nearbyint(((double)xb - (double)fx) * 256.0) / 256.0);
-        b = (T)(std::nearbyint(((double)yb - (double)fy) * 256.0) / 256.0);
+        a = (T)(std::floor(((double)xb - (double)fx) * 256.0 + 0.5) / 256.0);
+        b = (T)(std::floor(((double)yb - (double)fy) * 256.0 + 0.5) / 256.0);
     }
     const double ix = clampv((double)fx, -1.0, (double)W), iy = clampv((double)fy, -1.0, (double)H);
     const int i0 = clampv((int)ix, 0, W - 1), i1 = clampv((int)ix + 1, 0, W - 1);
