@@ -2,8 +2,10 @@
 
 Every translation unit is compiled in parallel with nvcc
 (``-gencode arch=compute_103a,code=sm_103a``) and linked into
-``gmvs_gb300/_lib/libgmvs_gb300.so``.  ``fusion.cu`` is compiled with
-``-fmad=false`` so its arithmetic rounds like the sequential host scan.
+``gmvs_gb300/_lib/libgmvs_gb300.so``.  Device code is compiled with
+``-fmad=false`` and host code with ``-ffp-contract=off``: every fused
+multiply-add is explicit, so results are reproducible bit for bit by a host
+implementation of the same arithmetic.
 """
 
 from __future__ import annotations
@@ -21,9 +23,12 @@ LIB_PATH = os.path.join(OUT_DIR, "libgmvs_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
-              "-I" + INCLUDE]
-CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-I" + INCLUDE]
+# -fmad=false: only explicit fused multiply-adds are fused, so device code
+# rounds exactly like the host restatement of the same arithmetic;
+# -ffp-contract=off does the same for host code on aarch64 and x86-64.
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler",
+              "-fvisibility=hidden", "-Xcompiler", "-ffp-contract=off", "-I" + INCLUDE]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-I" + INCLUDE]
 
 SOURCES = {
     "pm_f32.cu": [],
@@ -31,7 +36,7 @@ SOURCES = {
     "pm_qf16.cu": [],
     "pm_tex.cu": [],
     "runtime.cu": [],
-    "fusion.cu": ["-fmad=false"],
+    "fusion.cu": [],
     "prior.cpp": [],
 }
 

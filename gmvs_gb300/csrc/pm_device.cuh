@@ -6,6 +6,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "pmath.h"
 
 namespace gmvs {
 
@@ -80,11 +81,9 @@ struct SampTex {
     static constexpr bool kTex = true;
 };
 
-__device__ __forceinline__ float rcp_approx(float x) {
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
+// Correctly rounded reciprocal: u = X * (1 / Z) rounds exactly like the
+// host restatement of the projection.
+__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
 
 // -------------------------------------------------------- reference patch --
 // The bilateral weights, the reference samples and the reference moments do
@@ -109,7 +108,7 @@ struct Patch<0> {
 __device__ __forceinline__ float bilateral_weight(float xd, float yd, float pix, float center, float ss, float sc) {
     const float sd = sqrtf(xd * xd + yd * yd);
     const float cd = fabsf(pix - center);
-    return expf(-sd / (2.0f * ss * ss) - cd / (2.0f * sc * sc));
+    return pmath::expf_(-sd / (2.0f * ss * ss) - cd / (2.0f * sc * sc));
 }
 
 template <class S, int NS>
@@ -133,7 +132,6 @@ __device__ __forceinline__ void make_patch(Patch<NS>& P, const S& ref, const Dev
         }
 #pragma unroll
         for (int a = 0; a < NS; ++a) {
-            float c_w = 0.f, c_r = 0.f, c_rr = 0.f;
 #pragma unroll
             for (int b = 0; b < NS; ++b) {
                 const float r = ref.at((int)P.qx[a], (int)P.qy[b]);
@@ -142,26 +140,14 @@ __device__ __forceinline__ void make_patch(Patch<NS>& P, const S& ref, const Dev
                 const float wr = w * r;
                 P.w[a * NS + b] = w;
                 P.wr[a * NS + b] = wr;
-                if constexpr (S::kTex) {  // module A sums per window column
-                    c_r += wr;
-                    c_rr += wr * r;
-                    c_w += w;
-                } else {
-                    s_r += wr;
-                    s_rr += wr * r;
-                    s_w += w;
-                }
-            }
-            if constexpr (S::kTex) {
-                s_r += c_r;
-                s_rr += c_rr;
-                s_w += c_w;
+                s_r += wr;
+                s_rr = fmaf(wr, r, s_rr);
+                s_w += w;
             }
         }
     } else {
         P.center = ref.at(px, py);
         for (int i = -radius; i < radius + 1; i += inc) {
-            float c_w = 0.f, c_r = 0.f, c_rr = 0.f;
             for (int j = -radius; j < radius + 1; j += inc) {
                 int qx = px + i, qy = py + j;
                 if constexpr (!S::kTex) {
@@ -171,13 +157,11 @@ __device__ __forceinline__ void make_patch(Patch<NS>& P, const S& ref, const Dev
                 const float r = ref.at(qx, qy);
                 const float w =
                     bilateral_weight((float)i, (float)j, r, P.center, prm.sigma_spatial, prm.sigma_color);
-                c_r += w * r;
-                c_rr += w * r * r;
-                c_w += w;
+                const float wr = w * r;
+                s_r += wr;
+                s_rr = fmaf(wr, r, s_rr);
+                s_w += w;
             }
-            s_r += c_r;
-            s_rr += c_rr;
-            s_w += c_w;
         }
     }
     P.inv = 1.0f / s_w;
@@ -225,7 +209,7 @@ __device__ __forceinline__ float ncc_cost(const DevView& V, const DevParams& prm
             for (int bb = 0; bb < NS; ++bb) {
                 const float qy = P.qy[bb];
                 const float Z = fmaf(m7, qy, bz);
-                const float rz = rcp_approx(Z);
+                const float rz = rcp_rn(Z);
                 const float u = fmaf(m1, qy, bx) * rz;
                 const float v = fmaf(m4, qy, by) * rz;
                 const float s = src.sample(u, v);
@@ -250,10 +234,10 @@ __device__ __forceinline__ float ncc_cost(const DevView& V, const DevParams& prm
                 const float w =
                     bilateral_weight((float)i, (float)jj, r, P.center, prm.sigma_spatial, prm.sigma_color);
                 const float fqx = (float)qx, fqy = (float)qy;
-                const float Z = m6 * fqx + m7 * fqy + m8;
-                const float rz = rcp_approx(Z);
-                const float u = (m0 * fqx + m1 * fqy + m2) * rz;
-                const float v = (m3 * fqx + m4 * fqy + m5) * rz;
+                const float bx = fmaf(m0, fqx, m2), by = fmaf(m3, fqx, m5), bz = fmaf(m6, fqx, m8);
+                const float rz = rcp_rn(fmaf(m7, fqy, bz));
+                const float u = fmaf(m1, fqy, bx) * rz;
+                const float v = fmaf(m4, fqy, by) * rz;
                 const float s = src.sample(u, v);
                 const float ws = w * s;
                 ss += ws;
@@ -339,8 +323,8 @@ __device__ __forceinline__ float4 perturbed_normal(const DevCam& c, int px, int 
     const float a1 = (rng.uniform() - 0.5f) * pert;
     const float a2 = (rng.uniform() - 0.5f) * pert;
     const float a3 = (rng.uniform() - 0.5f) * pert;
-    const float s1 = sinf(a1), s2 = sinf(a2), s3 = sinf(a3);
-    const float c1 = cosf(a1), c2 = cosf(a2), c3 = cosf(a3);
+    const float s1 = pmath::sinf_(a1), s2 = pmath::sinf_(a2), s3 = pmath::sinf_(a3);
+    const float c1 = pmath::cosf_(a1), c2 = pmath::cosf_(a2), c3 = pmath::cosf_(a3);
     const float R0 = c2 * c3, R1 = c3 * s1 * s2 - c1 * s3, R2 = s1 * s3 + c1 * c3 * s2;
     const float R3 = c2 * s3, R4 = c1 * c3 + s1 * s2 * s3, R5 = c1 * s2 * s3 - c3 * s1;
     const float R6 = -s2, R7 = c2 * s1, R8 = c1 * c2;
@@ -385,9 +369,9 @@ __device__ __forceinline__ PriorK prior_k(const DevView& V) {
     return k;
 }
 __device__ __forceinline__ float restricted(const PriorK& k, float cost, float dd, float ac) {
-    const float ad = acosf(ac);
-    const float pr = k.gamma + expf(-dd * dd / k.two_dsq) * expf(-ad * ad / k.two_asq);
-    return expf(-cost * cost / k.beta) * pr;
+    const float ad = pmath::acosf_(ac);
+    const float pr = k.gamma + pmath::expf_(-dd * dd / k.two_dsq) * pmath::expf_(-ad * ad / k.two_asq);
+    return pmath::expf_(-cost * cost / k.beta) * pr;
 }
 
 // insertion sort, FindMinCostIndex / FindMaxCostIndex (patch_match_kernel.cu:5-37)
@@ -718,7 +702,7 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
     const uint32_t nb_sel[4] = {(flags & 1u) ? so[center - W] : 0u, (flags & 4u) ? so[center + W] : 0u,
                                 (flags & 16u) ? so[center - 1] : 0u, (flags & 64u) ? so[center + 1] : 0u};
     const float thr = prm.cost_thr[iter];
-    const float fallback = expf(thr * thr / (-0.32f));
+    const float fallback = pmath::expf_(thr * thr / (-0.32f));
     float prob_sum = 0.0f;
     for (int i = 0; i < N; ++i) {
         float pri = 0.0f;
@@ -729,7 +713,7 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
         for (int k = 0; k < 8; ++k) {
             const float c = CA(k, i);
             if (c < thr) {
-                tmpw += expf(c * c / (-0.18f));
+                tmpw += pmath::expf_(c * c / (-0.18f));
                 count++;
             }
             if (c > 1.2f) count_false++;

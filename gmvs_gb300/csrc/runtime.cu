@@ -12,6 +12,7 @@
 #include "errors.h"
 #include "kernels.h"
 #include "pm_device.cuh"
+#include "pmath.h"
 
 using namespace gmvs;
 
@@ -353,7 +354,7 @@ void fill_params(DevParams& P, const gmvs_params* p, int nmax) {
     P.nmax = nmax;
     // cost_threshold = 0.8 * expf(iter*iter / -90) (patch_match_kernel.cu:1143)
     for (int it = 0; it < kMaxIters; ++it)
-        P.cost_thr[it] = (float)(0.8 * (double)expf((float)(it * it) / (-90.0f)));
+        P.cost_thr[it] = (float)(0.8 * (double)pmath::expf_((float)(it * it) / (-90.0f)));
 }
 
 int num_sms() {

@@ -132,13 +132,13 @@ def render(planes: List[Plane], K, R, t, H: int, W: int, rng: np.random.Generato
     """Ray-cast one view: (uint8 image, depth, world normal, plane id)."""
     dev = device or torch.device("cpu")
     dt = torch.float64
-    Kt = torch.tensor(K, dtype=dt, device=dev)
     Rt = torch.tensor(R, dtype=dt, device=dev)
     tt = torch.tensor(t, dtype=dt, device=dev)
     C = -(Rt.T @ tt)
     ys, xs = torch.meshgrid(torch.arange(H, dtype=dt, device=dev), torch.arange(W, dtype=dt, device=dev),
                             indexing="ij")
-    pc = torch.stack([xs, ys, torch.ones_like(xs)], -1) @ torch.linalg.inv(Kt).T  # camera rays, z = 1
+    Kinv = torch.tensor(np.linalg.inv(np.asarray(K, np.float64)), dtype=dt, device=dev)
+    pc = torch.stack([xs, ys, torch.ones_like(xs)], -1) @ Kinv.T  # camera rays, z = 1
     dw = pc @ Rt                                                                  # world directions
     best = torch.full((H, W), float("inf"), dtype=dt, device=dev)
     pid = torch.full((H, W), -1, dtype=torch.int64, device=dev)

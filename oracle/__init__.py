@@ -55,12 +55,16 @@ def lib() -> ctypes.CDLL:
             "oracle_u01": (_f, [ctypes.c_uint32]),
             "oracle_ncc_costs": (_i, [_p, _i, _i, _i, _p, P, _p, _p, _p, _p, _i, _i]),
             "oracle_run_pass": (_i, [_p, _i, _i, _i, _p, _p, _p, _p, _p, _p, _p, P, _p, _p, _p, _p, _i]),
-            "oracle_fuse": (_i, [_p, _i, _i, _p, _i, _i, _p, _p, _p, _i, _f, _p, _p, _p]),
+            "oracle_fuse": (_i, [_p, _i, _i, _p, _i, _i, _p, _p, _p, _i, _f, _p, _p, _p, _p]),
             "oracle_build_prior": (_i, [_p, _i, _i, _p, _p, _p, _i, _f, _f, _p, _p, ctypes.POINTER(_i), _p, _i]),
             "oracle_delaunay": (_i, [_p, _i, _i, _p, _i]),
             "oracle_fusion_planar_mask": (_i, [_p, _p, _p, _i, _i, _i, _f, _f, _f, _p]),
             "oracle_filter_by_var_map": (_i, [_p, _p, _i, _i, _f, _p]),
             "oracle_sliding_window_normal": (_i, [_p, _p, _i, _i, _i, _p]),
+            "oracle_pm_expf": (_f, [_f]),
+            "oracle_pm_sinf": (_f, [_f]),
+            "oracle_pm_cosf": (_f, [_f]),
+            "oracle_pm_acosf": (_f, [_f]),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(L, name)
@@ -106,6 +110,12 @@ def philox4x32_10(ctr, key) -> np.ndarray:
     o = (ctypes.c_uint32 * 4)()
     lib().oracle_philox4x32_10(c, k, o)
     return np.array(list(o), dtype=np.uint32)
+
+
+def pm(name: str, xs) -> np.ndarray:
+    """The shared elementary function `name` (expf, sinf, cosf, acosf) on xs."""
+    fn = getattr(lib(), f"oracle_pm_{name}")
+    return np.array([fn(float(x)) for x in np.asarray(xs, np.float32)], np.float32)
 
 
 def u01(x: int) -> float:
@@ -163,10 +173,11 @@ def cos_threshold() -> float:
 
 
 def fuse(cam_args, ref_id: int, src_ids, depths: np.ndarray, normals: np.ndarray, masks: np.ndarray,
-         geom_consistent: int):
+         geom_consistent: int, with_hits: bool = False):
     """Fusion of one reference view.  depths [1+N, H, W], normals [1+N, H, W, 3]
     (ref, then sources), masks uint8 [V, H, W] updated in place.
-    Returns (depth, normal, count)."""
+    Returns (depth, normal, count); with_hits=True adds the number of
+    reference pixels written to each output pixel (> 1: a collision)."""
     d = np.ascontiguousarray(depths, np.float32)
     n = np.ascontiguousarray(normals, np.float32)
     assert masks.dtype == np.uint8 and masks.flags.c_contiguous
@@ -175,13 +186,14 @@ def fuse(cam_args, ref_id: int, src_ids, depths: np.ndarray, normals: np.ndarray
     od = np.zeros((H, W), np.float32)
     on = np.zeros((H, W, 3), np.float32)
     cnt = np.zeros((H, W), np.int32)
+    hits = np.zeros((H, W), np.int32)
     cams = cameras(cam_args)
     rc = lib().oracle_fuse(cams, n1 - 1, int(ref_id), _np_ptr(ids), H, W, _np_ptr(d), _np_ptr(n), _np_ptr(masks),
                            int(geom_consistent), ctypes.c_float(cos_threshold()), _np_ptr(od), _np_ptr(on),
-                           _np_ptr(cnt))
+                           _np_ptr(cnt), _np_ptr(hits))
     if rc != 0:
         raise RuntimeError(f"oracle_fuse failed ({rc})")
-    return od, on, cnt
+    return (od, on, cnt, hits) if with_hits else (od, on, cnt)
 
 
 def build_prior(cam_arg, depth: np.ndarray, cost: np.ndarray, superpixel, superpixel_filter: bool,

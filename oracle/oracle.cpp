@@ -9,10 +9,18 @@
 // Every routine cites the reference function it restates (paths relative to
 // the reference project).  Two sampling semantics are restated:
 //   * module B (gmvs/src/patch_match.cu): fp32 bilinear on global memory with
-//     truncate-then-clamp indexing, sequential NCC sums;
+//     truncate-then-clamp indexing;
 //   * module A (gmvs/lib/src/patch_match_kernel.cu): tex2D with linear
-//     filtering (8-bit fractional weights, clamped addressing), per-column
-//     partial NCC sums.
+//     filtering (8-bit fractional weights, clamped addressing).
+// Arithmetic.  The fp32 restatement uses one documented formulation, shared
+// with the CUDA kernels so both round identically: the homography is
+// H = A - b g^T with A = K_s R_rel K_r^-1 and b = K_s t_rel formed in FP64
+// and rounded once, projected coordinates are X * (1 / Z) with a correctly
+// rounded reciprocal, every fused multiply-add is explicit (std::fma), the
+// window moments are summed sequentially, and exp / sin / cos / acos come
+// from gmvs_gb300/csrc/pmath.h.  The reference chains the same algebra in
+// fp32 (ComputeHomography, patch_match_kernel.cu:262-360); the fp64 path
+// below restates that chain in double and serves as the FP64 oracle.
 // Deliberate, documented differences from the reference GPU code:
 //   * the RNG is Philox4x32-10 (Salmon et al., SC'11) instead of curand
 //     XORWOW; draws are consumed in the reference's order;
@@ -29,6 +37,8 @@
 #include <cstdint>
 #include <cstring>
 #include <vector>
+
+#include "../gmvs_gb300/csrc/pmath.h"
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -373,6 +383,42 @@ inline T tex2d_linear(const float* img, float x, float y, int H, int W) {
 }
 
 // ----------------------------------------------------------------- views --
+struct ViewConst {  // A = K_s R_rel K_r^-1, b = K_s t_rel (rounded from FP64)
+    float A[9];
+    float b[3];
+};
+
+// The FP64 formation of the per-view-pair homography constants.
+inline ViewConst view_consts(const Cam& r, const Cam& s) {
+    ViewConst vc;
+    double Cr[3];
+    for (int a = 0; a < 3; ++a)
+        Cr[a] = -((double)r.R[0 * 3 + a] * r.t[0] + (double)r.R[1 * 3 + a] * r.t[1] + (double)r.R[2 * 3 + a] * r.t[2]);
+    const double fx = r.K[0], fy = r.K[4], cx = r.K[2], cy = r.K[5];
+    const double Kinv[9] = {1.0 / fx, 0.0, -cx / fx, 0.0, 1.0 / fy, -cy / fy, 0.0, 0.0, 1.0};
+    double Cs[3], Rr[9], tr[3];
+    for (int a = 0; a < 3; ++a)
+        Cs[a] = -((double)s.R[0 * 3 + a] * s.t[0] + (double)s.R[1 * 3 + a] * s.t[1] + (double)s.R[2 * 3 + a] * s.t[2]);
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+            Rr[a * 3 + b] = (double)s.R[a * 3 + 0] * r.R[b * 3 + 0] + (double)s.R[a * 3 + 1] * r.R[b * 3 + 1] +
+                            (double)s.R[a * 3 + 2] * r.R[b * 3 + 2];
+    for (int a = 0; a < 3; ++a)
+        tr[a] = (double)s.R[a * 3 + 0] * (Cr[0] - Cs[0]) + (double)s.R[a * 3 + 1] * (Cr[1] - Cs[1]) +
+                (double)s.R[a * 3 + 2] * (Cr[2] - Cs[2]);
+    const double Ks[9] = {s.K[0], 0.0, s.K[2], 0.0, s.K[4], s.K[5], 0.0, 0.0, s.K[8]};
+    double KR[9];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+            KR[a * 3 + b] = Ks[a * 3 + 0] * Rr[0 * 3 + b] + Ks[a * 3 + 1] * Rr[1 * 3 + b] + Ks[a * 3 + 2] * Rr[2 * 3 + b];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+            vc.A[a * 3 + b] = (float)(KR[a * 3 + 0] * Kinv[0 * 3 + b] + KR[a * 3 + 1] * Kinv[1 * 3 + b] +
+                                      KR[a * 3 + 2] * Kinv[2 * 3 + b]);
+    for (int a = 0; a < 3; ++a) vc.b[a] = (float)(Ks[a * 3 + 0] * tr[0] + Ks[a * 3 + 1] * tr[1] + Ks[a * 3 + 2] * tr[2]);
+    return vc;
+}
+
 struct ViewSet {
     int H, W, N;  // N = number of source views
     const Cam* cams;       // [1 + N]
@@ -382,6 +428,11 @@ struct ViewSet {
     int patch_size, radius_increment;
     float sigma_spatial, sigma_color;
     int top_k;
+    std::vector<ViewConst> vc;  // per source view
+    void init_consts() {
+        vc.clear();
+        for (int j = 1; j <= N; ++j) vc.push_back(view_consts(cams[0], cams[j]));
+    }
     const float* img(int i) const { return images + (size_t)i * H * W; }
     const float* dep(int i) const { return depths + (size_t)i * H * W; }
 };
@@ -392,6 +443,12 @@ inline T bilateral_weight(T xd, T yd, T pix, T center, T ss, T sc) {
     const T sd = std::sqrt(xd * xd + yd * yd);
     const T cd = std::fabs(pix - center);
     return std::exp(-sd / ((T)2 * ss * ss) - cd / ((T)2 * sc * sc));
+}
+template <>
+inline float bilateral_weight<float>(float xd, float yd, float pix, float center, float ss, float sc) {
+    const float sd = std::sqrt(xd * xd + yd * yd);
+    const float cd = std::fabs(pix - center);
+    return pmath::expf_(-sd / (2.0f * ss * ss) - cd / (2.0f * sc * sc));
 }
 
 // ComputeBilateralNCC: module A (patch_match_kernel.cu:412-516) or module B
@@ -471,9 +528,75 @@ T bilateral_ncc(const ViewSet& vs, int src, int px, int py, const F4& pl) {
     return std::fmax((T)0, std::fmin(cost_max, (T)1 - cov / vrs));
 }
 
+// ComputeBilateralNCC in the shared fp32 formulation (see the file header):
+// module A (patch_match_kernel.cu:412-516) or module B (patch_match.cu:
+// 347-445) sampling, H = A - b g^T, X * (1 / Z), explicit fused
+// multiply-adds, sequential window sums in (x offset, y offset) order.
+inline float ncc_f32(const ViewSet& vs, int src, int px, int py, const F4& pl) {
+    const Cam& rc = vs.cams[0];
+    const Cam& sc = vs.cams[src];
+    const ViewConst& C = vs.vc[src - 1];
+    const float fx = rc.K[0], fy = rc.K[4], cx = rc.K[2], cy = rc.K[5];
+    const float iw = 1.0f / pl.w;
+    const float g[3] = {pl.x / fx * iw, pl.y / fy * iw, (pl.z - pl.x * cx / fx - pl.y * cy / fy) * iw};
+    float m[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) m[r * 3 + c] = std::fma(-C.b[r], g[c], C.A[r * 3 + c]);
+    const float fpx = (float)px, fpy = (float)py;
+    const float cz = m[6] * fpx + m[7] * fpy + m[8];
+    const float cu = (m[0] * fpx + m[1] * fpy + m[2]) / cz;
+    const float cv = (m[3] * fpx + m[4] * fpy + m[5]) / cz;
+    if (cu >= (float)sc.width || cu < 0.0f || cv >= (float)sc.height || cv < 0.0f) return 2.0f;
+    const int radius = vs.patch_size / 2;
+    const int Hh = vs.H, Ww = vs.W;
+    const float* ref = vs.img(0);
+    const float* sim = vs.img(src);
+    const bool tex = vs.sampler == 1;
+    const float center = tex ? tex2d_linear<float>(ref, fpx + 0.5f, fpy + 0.5f, Hh, Ww) : ref[py * Ww + px];
+    float s_w = 0.f, s_r = 0.f, s_rr = 0.f, ss = 0.f, sss = 0.f, srs = 0.f;
+    for (int i = -radius; i < radius + 1; i += vs.radius_increment) {
+        for (int j = -radius; j < radius + 1; j += vs.radius_increment) {
+            int qx = px + i, qy = py + j;
+            if (!tex) {
+                qx = clampv(qx, 0, Ww - 1);
+                qy = clampv(qy, 0, Hh - 1);
+            }
+            const float r = tex ? tex2d_linear<float>(ref, (float)qx + 0.5f, (float)qy + 0.5f, Hh, Ww)
+                                : ref[qy * Ww + qx];
+            const float w = bilateral_weight<float>((float)i, (float)j, r, center, vs.sigma_spatial, vs.sigma_color);
+            const float wr = w * r;
+            s_r += wr;
+            s_rr = std::fma(wr, r, s_rr);
+            s_w += w;
+            const float fqx = (float)qx, fqy = (float)qy;
+            const float bx = std::fma(m[0], fqx, m[2]), by = std::fma(m[3], fqx, m[5]), bz = std::fma(m[6], fqx, m[8]);
+            const float rz = 1.0f / std::fma(m[7], fqy, bz);
+            const float u = std::fma(m[1], fqy, bx) * rz;
+            const float v = std::fma(m[4], fqy, by) * rz;
+            const float s = tex ? tex2d_linear<float>(sim, u + 0.5f, v + 0.5f, Hh, Ww)
+                                : bilinear_clamp<float>(sim, u, v, Hh, Ww);
+            const float ws = w * s;
+            ss += ws;
+            sss = std::fma(ws, s, sss);
+            srs = std::fma(wr, s, srs);
+        }
+    }
+    const float inv = 1.0f / s_w;
+    const float mean_r = s_r * inv;
+    const float var_r = s_rr * inv - mean_r * mean_r;
+    const float sm = ss * inv;
+    const float sq = sss * inv;
+    const float sr = srs * inv;
+    const float var_s = sq - sm * sm;
+    if (var_r < 1e-5f || var_s < 1e-5f) return 2.0f;
+    const float cov = sr - mean_r * sm;
+    const float vrs = std::sqrt(var_r * var_s);
+    return std::fmax(0.0f, std::fmin(2.0f, 1.0f - cov / vrs));
+}
+
 // ComputeMultiViewCostVector (patch_match_kernel.cu:571-588)
 inline void cost_vector(const ViewSet& vs, int px, int py, const F4& pl, float* out) {
-    for (int i = 1; i <= vs.N; ++i) out[i - 1] = bilateral_ncc<float>(vs, i, px, py, pl);
+    for (int i = 1; i <= vs.N; ++i) out[i - 1] = ncc_f32(vs, i, px, py, pl);
 }
 
 // ComputeMultiViewInitialCostandSelectedViews (patch_match_kernel.cu:518-569)
@@ -548,8 +671,8 @@ inline F4 perturbed_normal(const Cam& c, int px, int py, const F4& n, Rng& rng, 
     const float a1 = (rng.uniform() - 0.5f) * pert;
     const float a2 = (rng.uniform() - 0.5f) * pert;
     const float a3 = (rng.uniform() - 0.5f) * pert;
-    const float s1 = std::sin(a1), s2 = std::sin(a2), s3 = std::sin(a3);
-    const float c1 = std::cos(a1), c2 = std::cos(a2), c3 = std::cos(a3);
+    const float s1 = pmath::sinf_(a1), s2 = pmath::sinf_(a2), s3 = pmath::sinf_(a3);
+    const float c1 = pmath::cosf_(a1), c2 = pmath::cosf_(a2), c3 = pmath::cosf_(a3);
     float R[9];
     R[0] = c2 * c3;
     R[1] = c3 * s1 * s2 - c1 * s3;
@@ -648,10 +771,10 @@ inline PriorConsts prior_consts(const oracle_params& p) {
     return k;
 }
 inline float restricted(const PriorConsts& k, float cost, float depth_diff, float angle_cos) {
-    const float angle_diff = std::acos(angle_cos);
-    const float prior = k.gamma + std::exp(-depth_diff * depth_diff / k.two_depth_sigma_sq) *
-                                      std::exp(-angle_diff * angle_diff / k.two_angle_sigma_sq);
-    return std::exp(-cost * cost / k.beta) * prior;
+    const float angle_diff = pmath::acosf_(angle_cos);
+    const float prior = k.gamma + pmath::expf_(-depth_diff * depth_diff / k.two_depth_sigma_sq) *
+                                      pmath::expf_(-angle_diff * angle_diff / k.two_angle_sigma_sq);
+    return pmath::expf_(-cost * cost / k.beta) * prior;
 }
 
 // One pixel of a half-sweep: CheckerboardPropagation (patch_match_kernel.cu:
@@ -849,7 +972,7 @@ void sweep_pixel(const PassCtx& ctx, int px, int py, int iter, int colour, float
         float tmpw = 0;
         for (int j = 0; j < 8; ++j) {
             if (cost_array[j][i] < cost_threshold) {
-                tmpw += std::exp(cost_array[j][i] * cost_array[j][i] / (-0.18f));
+                tmpw += pmath::expf_(cost_array[j][i] * cost_array[j][i] / (-0.18f));
                 count++;
             }
             if (cost_array[j][i] > 1.2f) count_false++;
@@ -857,7 +980,7 @@ void sweep_pixel(const PassCtx& ctx, int px, int py, int iter, int colour, float
         if (count > 2 && count_false < 3)
             probs[i] = tmpw / count;
         else if (count_false < 3)
-            probs[i] = std::exp(cost_threshold * cost_threshold / (-0.32f));
+            probs[i] = pmath::expf_(cost_threshold * cost_threshold / (-0.32f));
         probs[i] = probs[i] * priors[i];
     }
     pdf_to_cdf(probs, N);
@@ -989,7 +1112,7 @@ void sweep_pixel(const PassCtx& ctx, int px, int py, int iter, int colour, float
             float cvk[kMaxNgb];
             for (int j = 0; j < N; ++j) cvk[j] = 0.0f;
             for (int j = 0; j < N; ++j)
-                if (view_weights[j] > 0) cvk[j] = bilateral_ncc<float>(vs, j + 1, px, py, cand);
+                if (view_weights[j] > 0) cvk[j] = ncc_f32(vs, j + 1, px, py, cand);
             float tc = 0.0f;
             for (int j = 0; j < N; ++j) {
                 if (view_weights[j] > 0) {
@@ -1076,6 +1199,12 @@ void oracle_philox4x32_10(const uint32_t* ctr, const uint32_t* key, uint32_t* ou
 
 float oracle_u01(uint32_t x) { return u01(x); }
 
+// The shared elementary functions, for their accuracy tests.
+float oracle_pm_expf(float x) { return pmath::expf_(x); }
+float oracle_pm_sinf(float x) { return pmath::sinf_(x); }
+float oracle_pm_cosf(float x) { return pmath::cosf_(x); }
+float oracle_pm_acosf(float x) { return pmath::acosf_(x); }
+
 // Per-view NCC costs of given camera-frame planes (float4 per pixel) and the
 // initial multi-view cost / selected views.  fp64 != 0 evaluates the NCC in
 // double precision (the FP64 oracle).
@@ -1084,7 +1213,8 @@ int oracle_ncc_costs(const Cam* cams, int num_src, int H, int W, const float* im
                      int nthreads) {
     if (num_src < 1 || num_src > kMaxNgb || H < 1 || W < 1) return 1;
     ViewSet vs{H, W, num_src, cams, images, nullptr, prm->sampler, prm->patch_size, prm->radius_increment,
-               prm->sigma_spatial, prm->sigma_color, prm->top_k};
+               prm->sigma_spatial, prm->sigma_color, prm->top_k, {}};
+    vs.init_consts();
     const F4* pl = reinterpret_cast<const F4*>(planes);
     const int nt = nthreads_or_default(nthreads);
 #pragma omp parallel for schedule(dynamic, 4) num_threads(nt)
@@ -1096,7 +1226,7 @@ int oracle_ncc_costs(const Cam* cams, int num_src, int H, int W, const float* im
                 if (fp64)
                     cv[s - 1] = (float)bilateral_ncc<double>(vs, s, x, y, pl[c]);
                 else
-                    cv[s - 1] = bilateral_ncc<float>(vs, s, x, y, pl[c]);
+                    cv[s - 1] = ncc_f32(vs, s, x, y, pl[c]);
                 if (costs) costs[(size_t)(s - 1) * H * W + c] = cv[s - 1];
             }
             uint32_t sel = 0;
@@ -1125,7 +1255,8 @@ int oracle_run_pass(const Cam* cams, int num_src, int H, int W, const float* ima
     if (prm->init_kind == 1 && (!init_planes || !init_costs)) return 1;
     PassCtx ctx;
     ctx.vs = ViewSet{H, W, num_src, cams, images, depths, prm->sampler, prm->patch_size, prm->radius_increment,
-                     prm->sigma_spatial, prm->sigma_color, prm->top_k};
+                     prm->sigma_spatial, prm->sigma_color, prm->top_k, {}};
+    ctx.vs.init_consts();
     ctx.prm = *prm;
     ctx.prior_planes = reinterpret_cast<const F4*>(prior_planes);
     ctx.prior_masks = prior_masks;
@@ -1139,7 +1270,7 @@ int oracle_run_pass(const Cam* cams, int num_src, int H, int W, const float* ima
 
     for (int it = 0; it < prm->max_iterations; ++it) {
         // cost_threshold = 0.8 * expf(iter*iter / -90) (patch_match_kernel.cu:1143)
-        const float thr = (float)(0.8 * (double)std::exp((float)(it * it) / (-90.0f)));
+        const float thr = (float)(0.8 * (double)pmath::expf_((float)(it * it) / (-90.0f)));
         for (int colour = 0; colour < 2; ++colour) {
             b = a;
 #pragma omp parallel for schedule(dynamic, 2) num_threads(nt)
@@ -1192,10 +1323,11 @@ int oracle_run_pass(const Cam* cams, int num_src, int H, int W, const float* ima
 // or d > cos_thresh" with cos_thresh supplied by the caller.
 int oracle_fuse(const Cam* cams, int num_src, int ref_id, const int32_t* src_ids, int H, int W, const float* depths,
                 const float* normals, uint8_t* masks, int geom_consistent, float cos_thresh, float* out_depth,
-                float* out_normal, int32_t* out_count) {
+                float* out_normal, int32_t* out_count, int32_t* out_hits) {
     const size_t HW = (size_t)H * W;
     std::memset(out_depth, 0, HW * sizeof(float));
     std::memset(out_normal, 0, HW * 3 * sizeof(float));
+    if (out_hits) std::memset(out_hits, 0, HW * sizeof(int32_t));
     const Cam& rc = cams[0];
     std::vector<uint8_t> pending;  // masks are applied after the scan: the
                                    // kernel reads only masks[ref] and writes
@@ -1263,6 +1395,7 @@ int oracle_fuse(const Cam* cams, int num_src, int ref_id, const int32_t* src_ids
                 const int pr = f2i_rz(pv + 0.5f), pc = f2i_rz(pu + 0.5f);
                 if (pc >= 0 && pc < W && pr >= 0 && pr < H && pdd > 0.001f) {
                     const size_t pi = (size_t)pr * W + pc;
+                    if (out_hits) out_hits[pi] += 1;
                     out_depth[pi] = pdd;
                     out_normal[pi * 3 + 0] = cn[0];
                     out_normal[pi * 3 + 1] = cn[1];

@@ -100,3 +100,22 @@ def test_fusion_of_exact_maps(orc, small):
     ids2 = [ref2] + src2
     _, _, cnt2 = orc.fuse(cam_args(small, ids2), ref2, src2, small.depths[ids2], small.normals[ids2], masks, 3)
     assert np.all(cnt2[masks[ref2] > 0] == -1)
+
+
+def _ulp_err(got, exact):
+    got = got.astype(np.float64)
+    ulp = np.spacing(np.abs(exact).astype(np.float32)).astype(np.float64)
+    return np.abs(got - exact) / np.maximum(ulp, 1e-45)
+
+
+def test_shared_elementary_functions_accuracy(orc):
+    rng = np.random.default_rng(0)
+    x = np.concatenate([rng.uniform(-87, 88, 4000), rng.uniform(-2, 2, 4000), [0.0, -1e-8, 1e-8]]).astype(np.float32)
+    assert _ulp_err(orc.pm("expf", x), np.exp(x.astype(np.float64))).max() <= 2
+    a = rng.uniform(-1, 1, 4000).astype(np.float32)
+    assert _ulp_err(orc.pm("sinf", a), np.sin(a.astype(np.float64)))[np.abs(a) > 1e-30].max() <= 2
+    assert _ulp_err(orc.pm("cosf", a), np.cos(a.astype(np.float64))).max() <= 2
+    c = np.concatenate([rng.uniform(-1, 1, 4000), [-1.0, -0.5, 0.0, 0.5, 1.0]]).astype(np.float32)
+    assert _ulp_err(orc.pm("acosf", c), np.arccos(c.astype(np.float64)))[c < 0.999].max() <= 4
+    assert np.isnan(orc.pm("acosf", [1.0000001, -1.5])).all()
+    assert orc.pm("expf", [-200.0])[0] == 0.0 and np.isinf(orc.pm("expf", [100.0])[0])
