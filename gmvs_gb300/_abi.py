@@ -96,9 +96,10 @@ _lib = None
 
 
 def library_path() -> str:
+    """The in-tree library, or the variant named by GMVS_GB300_LIB."""
     from .build import LIB_PATH
 
-    return LIB_PATH
+    return os.environ.get("GMVS_GB300_LIB", LIB_PATH)
 
 
 def lib() -> ctypes.CDLL:

@@ -62,8 +62,8 @@ def is_stale() -> bool:
     return any(os.path.getmtime(f) > t for f in _inputs())
 
 
-def _compile(src: str, extra: list[str], verbose: bool) -> str:
-    obj = os.path.join(OUT_DIR, "obj", src + ".o")
+def _compile(src: str, extra: list[str], verbose: bool, out_dir: str = OUT_DIR) -> str:
+    obj = os.path.join(out_dir, "obj", src + ".o")
     path = os.path.join(CSRC, src)
     if src.endswith(".cpp"):
         cmd = [os.environ.get("CXX", "g++"), *CXX_FLAGS, "-c", path, "-o", obj]
@@ -77,20 +77,24 @@ def _compile(src: str, extra: list[str], verbose: bool) -> str:
     return obj
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile and link the library if any input changed; return its path."""
-    if not force and not is_stale():
+def build(force: bool = False, verbose: bool = False, defines: tuple = (), out_dir: str = OUT_DIR) -> str:
+    """Compile and link the library if any input changed; return its path.
+    `defines` (e.g. ("GMVS_MIN_BLOCKS=3",)) and `out_dir` build a variant
+    library elsewhere, for tuning experiments."""
+    lib_path = os.path.join(out_dir, "libgmvs_gb300.so")
+    if not force and not defines and out_dir == OUT_DIR and not is_stale():
         return LIB_PATH
-    os.makedirs(os.path.join(OUT_DIR, "obj"), exist_ok=True)
+    os.makedirs(os.path.join(out_dir, "obj"), exist_ok=True)
+    extra_d = ["-D" + d for d in defines]
     with ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose), SOURCES.items()))
-    tmp = LIB_PATH + ".tmp"
+        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1] + extra_d, verbose, out_dir), SOURCES.items()))
+    tmp = lib_path + ".tmp"
     cmd = [_nvcc(), *ARCH, "-shared", "-o", tmp, *objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"linking libgmvs_gb300.so failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

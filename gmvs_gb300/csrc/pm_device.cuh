@@ -81,28 +81,49 @@ struct SampTex {
     static constexpr bool kTex = true;
 };
 
-// Correctly rounded reciprocal: u = X * (1 / Z) rounds exactly like the
-// host restatement of the projection.
-__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
+// Correctly rounded reciprocal: the hardware approximation refined by one
+// Newton step with fused multiply-adds.  Checked on a GB300 against the IEEE
+// round-to-nearest reciprocal for every significand at 30 binary exponents
+// between 2^-125 and 2^125 of both signs: identical.  Outside that range
+// (and for 0, inf, NaN) the IEEE reciprocal is used.
+__device__ __forceinline__ float rcp_rn(float x) {
+    const float ax = fabsf(x);
+    if (!(ax >= 2.35098870e-38f && ax <= 4.25352959e+37f)) return __frcp_rn(x);  // 2^-125, 2^125
+    float y;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    const float e = __fmaf_rn(-x, y, 1.0f);
+    return __fmaf_rn(y, e, y);
+}
 
 // -------------------------------------------------------- reference patch --
-// The bilateral weights, the reference samples and the reference moments do
-// not depend on the hypothesis (ComputeBilateralWeight depends only on the
-// window offset and |I_ref - I_ref(centre)|, patch_match_kernel.cu:397-410),
-// so they are formed once per pixel per launch.  NS = samples per axis
-// (6 for the default 11x11 window with stride 2); NS = 0 is the generic path
-// that recomputes them per sample for other window shapes.
+// A pixel is evaluated by two adjacent lanes of a warp.  Lane half h = 0
+// takes the left half of the window columns (x offsets), h = 1 the right
+// half; every window sum is (left half) + (right half), combined with one
+// shuffle.  The bilateral weights, the reference samples and the reference
+// moments do not depend on the hypothesis (ComputeBilateralWeight depends
+// only on the window offset and |I_ref - I_ref(centre)|,
+// patch_match_kernel.cu:397-410), so they are formed once per pixel and
+// launch.  NS = samples per axis (6 for the default 11x11 window with
+// stride 2); NS = 0 is the generic path that recomputes them per sample.
+struct Pair {
+    int h;          // which half of the window columns
+    unsigned mask;  // the two lanes of the pixel
+};
+__device__ __forceinline__ Pair make_pair(unsigned lane) { return Pair{(int)(lane & 1u), 3u << (lane & 30u)}; }
+// left + right: lane 0 adds (l, r), lane 1 adds (r, l); IEEE addition commutes
+__device__ __forceinline__ float pair_sum(const Pair& q, float v) { return v + __shfl_xor_sync(q.mask, v, 1); }
+
 template <int NS>
 struct Patch {
-    float w[NS * NS];
-    float wr[NS * NS];
-    float qx[NS];
-    float qy[NS];
+    static constexpr int NC = NS / 2;  // columns per lane (NS even)
+    float w[NC * NS];
+    float wr[NC * NS];
     float inv, mean_r, var_r;
 };
 template <>
 struct Patch<0> {
     float center, inv, mean_r, var_r;
+    int c0, c1;  // this lane's window columns
 };
 
 __device__ __forceinline__ float bilateral_weight(float xd, float yd, float pix, float center, float ss, float sc) {
@@ -111,52 +132,49 @@ __device__ __forceinline__ float bilateral_weight(float xd, float yd, float pix,
     return pmath::expf_(-sd / (2.0f * ss * ss) - cd / (2.0f * sc * sc));
 }
 
+template <class S>
+__device__ __forceinline__ int window_coord(int p, int off, int n) {
+    if constexpr (S::kTex) return p + off;
+    else return min(max(p + off, 0), n - 1);
+}
+
 template <class S, int NS>
 __device__ __forceinline__ void make_patch(Patch<NS>& P, const S& ref, const DevView& V, const DevParams& prm, int px,
-                                           int py) {
+                                           int py, const Pair& q) {
     const int radius = prm.patch_size / 2;
     const int inc = prm.radius_increment;
     float s_w = 0.f, s_r = 0.f, s_rr = 0.f;
     if constexpr (NS > 0) {
+        constexpr int NC = NS / 2;
         const float center = ref.at(px, py);
 #pragma unroll
-        for (int a = 0; a < NS; ++a) {
-            const int off = -radius + a * inc;
-            if constexpr (S::kTex) {
-                P.qx[a] = (float)(px + off);
-                P.qy[a] = (float)(py + off);
-            } else {
-                P.qx[a] = (float)min(max(px + off, 0), V.W - 1);
-                P.qy[a] = (float)min(max(py + off, 0), V.H - 1);
-            }
-        }
-#pragma unroll
-        for (int a = 0; a < NS; ++a) {
+        for (int al = 0; al < NC; ++al) {
+            const int qx = window_coord<S>(px, -radius + (q.h * NC + al) * inc, V.W);
 #pragma unroll
             for (int b = 0; b < NS; ++b) {
-                const float r = ref.at((int)P.qx[a], (int)P.qy[b]);
-                const float w = bilateral_weight((float)(-radius + a * inc), (float)(-radius + b * inc), r, center,
-                                                 prm.sigma_spatial, prm.sigma_color);
+                const float r = ref.at(qx, window_coord<S>(py, -radius + b * inc, V.H));
+                const float w = bilateral_weight((float)(-radius + (q.h * NC + al) * inc), (float)(-radius + b * inc),
+                                                 r, center, prm.sigma_spatial, prm.sigma_color);
                 const float wr = w * r;
-                P.w[a * NS + b] = w;
-                P.wr[a * NS + b] = wr;
+                P.w[al * NS + b] = w;
+                P.wr[al * NS + b] = wr;
                 s_r += wr;
                 s_rr = fmaf(wr, r, s_rr);
                 s_w += w;
             }
         }
     } else {
+        const int n = (2 * radius) / inc + 1;
+        const int half = (n + 1) / 2;
+        P.c0 = q.h ? half : 0;
+        P.c1 = q.h ? n : half;
         P.center = ref.at(px, py);
-        for (int i = -radius; i < radius + 1; i += inc) {
-            for (int j = -radius; j < radius + 1; j += inc) {
-                int qx = px + i, qy = py + j;
-                if constexpr (!S::kTex) {
-                    qx = min(max(qx, 0), V.W - 1);
-                    qy = min(max(qy, 0), V.H - 1);
-                }
-                const float r = ref.at(qx, qy);
-                const float w =
-                    bilateral_weight((float)i, (float)j, r, P.center, prm.sigma_spatial, prm.sigma_color);
+        for (int a = P.c0; a < P.c1; ++a) {
+            const int i = -radius + a * inc;
+            for (int b = 0; b < n; ++b) {
+                const int j = -radius + b * inc;
+                const float r = ref.at(window_coord<S>(px, i, V.W), window_coord<S>(py, j, V.H));
+                const float w = bilateral_weight((float)i, (float)j, r, P.center, prm.sigma_spatial, prm.sigma_color);
                 const float wr = w * r;
                 s_r += wr;
                 s_rr = fmaf(wr, r, s_rr);
@@ -164,6 +182,9 @@ __device__ __forceinline__ void make_patch(Patch<NS>& P, const S& ref, const Dev
             }
         }
     }
+    s_w = pair_sum(q, s_w);
+    s_r = pair_sum(q, s_r);
+    s_rr = pair_sum(q, s_rr);
     P.inv = 1.0f / s_w;
     P.mean_r = s_r * P.inv;
     P.var_r = s_rr * P.inv - P.mean_r * P.mean_r;
@@ -184,10 +205,11 @@ __device__ __forceinline__ Hyp make_hyp(const DevCam& rc, float4 pl) {
 }
 
 // Bilateral NCC of one hypothesis against source j (0-based): ComputeBilateralNCC
-// (patch_match_kernel.cu:412-516; gmvs/src/patch_match.cu:347-445).
+// (patch_match_kernel.cu:412-516; gmvs/src/patch_match.cu:347-445).  Both
+// lanes of the pair return the same value.
 template <class S, int NS>
 __device__ __forceinline__ float ncc_cost(const DevView& V, const DevParams& prm, int j, const Hyp& h,
-                                          const Patch<NS>& P, int px, int py) {
+                                          const Patch<NS>& P, int px, int py, const Pair& q) {
     const float* A = V.A[j];
     const float* b = V.b[j];
     const float m0 = fmaf(-b[0], h.g0, A[0]), m1 = fmaf(-b[0], h.g1, A[1]), m2 = fmaf(-b[0], h.g2, A[2]);
@@ -201,40 +223,42 @@ __device__ __forceinline__ float ncc_cost(const DevView& V, const DevParams& prm
     const S src(V, j + 1);
     float ss = 0.f, sss = 0.f, srs = 0.f;
     if constexpr (NS > 0) {
+        constexpr int NC = NS / 2;
+        const int radius = prm.patch_size / 2;
+        const int inc = prm.radius_increment;
 #pragma unroll
-        for (int a = 0; a < NS; ++a) {
-            const float qx = P.qx[a];
+        for (int al = 0; al < NC; ++al) {
+            const float qx = (float)window_coord<S>(px, -radius + (q.h * NC + al) * inc, V.W);
             const float bx = fmaf(m0, qx, m2), by = fmaf(m3, qx, m5), bz = fmaf(m6, qx, m8);
 #pragma unroll
             for (int bb = 0; bb < NS; ++bb) {
-                const float qy = P.qy[bb];
-                const float Z = fmaf(m7, qy, bz);
-                const float rz = rcp_rn(Z);
+                const float qy = (float)window_coord<S>(py, -radius + bb * inc, V.H);
+                const float rz = rcp_rn(fmaf(m7, qy, bz));
                 const float u = fmaf(m1, qy, bx) * rz;
                 const float v = fmaf(m4, qy, by) * rz;
                 const float s = src.sample(u, v);
-                const float ws = P.w[a * NS + bb] * s;
+                const float ws = P.w[al * NS + bb] * s;
                 ss += ws;
                 sss = fmaf(ws, s, sss);
-                srs = fmaf(P.wr[a * NS + bb], s, srs);
+                srs = fmaf(P.wr[al * NS + bb], s, srs);
             }
         }
     } else {
         const int radius = prm.patch_size / 2;
         const int inc = prm.radius_increment;
+        const int n = (2 * radius) / inc + 1;
         const S ref(V, 0);
-        for (int i = -radius; i < radius + 1; i += inc) {
-            for (int jj = -radius; jj < radius + 1; jj += inc) {
-                int qx = px + i, qy = py + jj;
-                if constexpr (!S::kTex) {
-                    qx = min(max(qx, 0), V.W - 1);
-                    qy = min(max(qy, 0), V.H - 1);
-                }
-                const float r = ref.at(qx, qy);
+        for (int a = P.c0; a < P.c1; ++a) {
+            const int i = -radius + a * inc;
+            const float fqx = (float)window_coord<S>(px, i, V.W);
+            const float bx = fmaf(m0, fqx, m2), by = fmaf(m3, fqx, m5), bz = fmaf(m6, fqx, m8);
+            for (int bb = 0; bb < n; ++bb) {
+                const int jj = -radius + bb * inc;
+                const int qy = window_coord<S>(py, jj, V.H);
+                const float r = ref.at((int)fqx, qy);
                 const float w =
                     bilateral_weight((float)i, (float)jj, r, P.center, prm.sigma_spatial, prm.sigma_color);
-                const float fqx = (float)qx, fqy = (float)qy;
-                const float bx = fmaf(m0, fqx, m2), by = fmaf(m3, fqx, m5), bz = fmaf(m6, fqx, m8);
+                const float fqy = (float)qy;
                 const float rz = rcp_rn(fmaf(m7, fqy, bz));
                 const float u = fmaf(m1, fqy, bx) * rz;
                 const float v = fmaf(m4, fqy, by) * rz;
@@ -246,6 +270,9 @@ __device__ __forceinline__ float ncc_cost(const DevView& V, const DevParams& prm
             }
         }
     }
+    ss = pair_sum(q, ss);
+    sss = pair_sum(q, sss);
+    srs = pair_sum(q, srs);
     const float sm = ss * P.inv;
     const float sq = sss * P.inv;
     const float sr = srs * P.inv;
@@ -400,10 +427,12 @@ __device__ __forceinline__ int find_max_idx8(const float* c) {
 
 // ------------------------------------------------------------------ init --
 // One pixel of RandomInitialization (patch_match_kernel.cu:1467-1577) or of
-// module B's initialization (gmvs/src/patch_match.cu:1046-1082).  `cv` is
-// this thread's shared-memory row (stride nthr), 2 * nmax floats.
+// module B's initialization (gmvs/src/patch_match.cu:1046-1082), evaluated by
+// a lane pair.  `cv` is the pixel's shared-memory slot (stride npix),
+// 2 * nmax floats; both lanes write the same values.
 template <class S, int NS>
-__device__ void init_pixel(const DevView& V, const DevParams& prm, int px, int py, float* cv, int nthr) {
+__device__ void init_pixel(const DevView& V, const DevParams& prm, int px, int py, float* cv, int npix,
+                           const Pair& q) {
     const int W = V.W, N = V.N;
     const int c = py * W + px;
     const DevCam& rc = V.cam[0];
@@ -437,50 +466,55 @@ __device__ void init_pixel(const DevView& V, const DevParams& prm, int px, int p
         pl.w = distance_to_origin(rc, px, py, depth, pl);
     }
     Patch<NS> P;
-    make_patch<S, NS>(P, S(V, 0), V, prm, px, py);
+    make_patch<S, NS>(P, S(V, 0), V, prm, px, py, q);
     const Hyp h = make_hyp(rc, pl);
     int valid = 0;
     for (int i = 0; i < N; ++i) {
-        const float v = ncc_cost<S, NS>(V, prm, i, h, P, px, py);
-        cv[i * nthr] = v;
-        cv[(prm.nmax + i) * nthr] = v;
+        const float v = ncc_cost<S, NS>(V, prm, i, h, P, px, py, q);
+        cv[i * npix] = v;
+        cv[(prm.nmax + i) * npix] = v;
         if (v < 2.0f) valid++;
     }
     // ComputeMultiViewInitialCostandSelectedViews (patch_match_kernel.cu:518-569)
-    float* srt = cv + prm.nmax * nthr;
-    for (int i = 1; i < N; i++) {
-        const float tmp = srt[i * nthr];
-        int j = i;
-        for (; j >= 1 && tmp < srt[(j - 1) * nthr]; j--) srt[j * nthr] = srt[(j - 1) * nthr];
-        srt[j * nthr] = tmp;
+    float* srt = cv + prm.nmax * npix;
+    if (q.h == 0) {
+        for (int i = 1; i < N; i++) {
+            const float tmp = srt[i * npix];
+            int j = i;
+            for (; j >= 1 && tmp < srt[(j - 1) * npix]; j--) srt[j * npix] = srt[(j - 1) * npix];
+            srt[j * npix] = tmp;
+        }
+        uint32_t sel = 0;
+        float cost = 2.0f;
+        const int top_k = min(valid, prm.top_k);
+        if (top_k > 0) {
+            float acc = 0.0f;
+            for (int i = 0; i < top_k; ++i) acc += srt[i * npix];
+            const float thr = srt[(top_k - 1) * npix];
+            for (int i = 0; i < N; ++i)
+                if (cv[i * npix] <= thr) sel |= 1u << i;
+            cost = acc / (float)top_k;
+        }
+        V.plane[0][c] = pl;
+        V.cost[0][c] = cost;
+        V.sel[0][c] = sel;
     }
-    uint32_t sel = 0;
-    float cost = 2.0f;
-    const int top_k = min(valid, prm.top_k);
-    if (top_k > 0) {
-        float acc = 0.0f;
-        for (int i = 0; i < top_k; ++i) acc += srt[i * nthr];
-        const float thr = srt[(top_k - 1) * nthr];
-        for (int i = 0; i < N; ++i)
-            if (cv[i * nthr] <= thr) sel |= 1u << i;
-        cost = acc / (float)top_k;
-    }
-    V.plane[0][c] = pl;
-    V.cost[0][c] = cost;
-    V.sel[0][c] = sel;
 }
 
 // --------------------------------------------------------------- sweep --
 // One pixel of a half-sweep: CheckerboardPropagation (patch_match_kernel.cu:
 // 813-1351; gmvs/src/patch_match.cu:678-1041) then PlaneHypothesisRefinement
-// (patch_match_kernel.cu:684-811; gmvs/src/patch_match.cu:595-676).
-// Reads the state at the start of the half-sweep (buffer `same` for this
-// colour, `opp` for the other) and writes the pixel to buffer `outb`.
-// `my` is this thread's shared-memory slot (stride nthr): the 8 x nmax cost
-// matrix followed by nmax view weights.
+// (patch_match_kernel.cu:684-811; gmvs/src/patch_match.cu:595-676), by a lane
+// pair.  Reads the state at the start of the half-sweep (buffer `same` for
+// this colour, `opp` for the other) and writes the pixel to buffer `outb`.
+// `my` is the pixel's shared-memory slot (stride npix): the 8 x nmax cost
+// matrix, nmax view weights, then the cold per-pixel state (neighbour
+// positions, candidate final costs, refinement planes).  All 14 hypotheses
+// (8 neighbours, the current plane, 5 refinement candidates) go through one
+// NCC loop.
 template <class S, int NS>
 __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int py, int iter, int colour, float* my,
-                            int nthr) {
+                            int npix, const Pair& q) {
     const int W = V.W, H = V.H, N = V.N, nmax = prm.nmax;
     const int center = py * W + px;
     const int same = iter & 1;
@@ -491,428 +525,436 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
     const DevCam& rc = V.cam[0];
     const bool geom = prm.sweep_kind == GMVS_SWEEP_GEOM;
     const bool prior_mode = prm.sweep_kind == GMVS_SWEEP_PRIOR;
-#define CA(k, i) my[((k) * nmax + (i)) * nthr]
-#define VW(i) my[(8 * nmax + (i)) * nthr]
+#define CA(k, i) my[((k) * nmax + (i)) * npix]
+#define VW(i) my[(8 * nmax + (i)) * npix]
+#define POS(k) (*reinterpret_cast<int*>(&my[(9 * nmax + (k)) * npix]))
+#define FC(k) my[(9 * nmax + 8 + (k)) * npix]
+#define PL4(slot, c) my[(9 * nmax + 16 + 4 * (slot) + (c)) * npix]
 
     DevRng rng(prm.seed_lo, prm.seed_hi, (uint32_t)center, (uint32_t)V.stream_id,
                phase_of(prm.pass_index, 1 + 2 * iter + colour));
     Patch<NS> P;
-    make_patch<S, NS>(P, S(V, 0), V, prm, px, py);
+    make_patch<S, NS>(P, S(V, 0), V, prm, px, py, q);
 
     // Adaptive checkerboard sampling.  pos = linear index; the buffer of a
     // candidate follows from its offset parity (odd = other colour).
     int pos[8];
     unsigned flags = 0u, fromsame = 0u;
-    float cmin;
-    int cminp;
-    bool csame;
-    // up_far (odd offsets only)
-    if (py > 2) {
-        flags |= 1u << 1;
-        cminp = center - 3 * W;
-        cmin = co[cminp];
-        for (int i = 1; i < 11; ++i)
-            if (py > 2 + 2 * i) {
-                const int t = center - 3 * W - 2 * i * W;
-                const float v = co[t];
-                if (v < cmin) {
-                    cmin = v;
-                    cminp = t;
-                }
-            }
-        pos[1] = cminp;
-    }
-    if (py < H - 3) {  // down_far
-        flags |= 1u << 3;
-        cminp = center + 3 * W;
-        cmin = co[cminp];
-        for (int i = 1; i < 11; ++i)
-            if (py < H - 3 - 2 * i) {
-                const int t = center + 3 * W + 2 * i * W;
-                const float v = co[t];
-                if (v < cmin) {
-                    cmin = v;
-                    cminp = t;
-                }
-            }
-        pos[3] = cminp;
-    }
-    if (px > 2) {  // left_far
-        flags |= 1u << 5;
-        cminp = center - 3;
-        cmin = co[cminp];
-        for (int i = 1; i < 11; ++i)
-            if (px > 2 + 2 * i) {
-                const int t = center - 3 - 2 * i;
-                const float v = co[t];
-                if (v < cmin) {
-                    cmin = v;
-                    cminp = t;
-                }
-            }
-        pos[5] = cminp;
-    }
-    if (px < W - 3) {  // right_far keeps the maximum (patch_match_kernel.cu:954)
-        flags |= 1u << 7;
-        cminp = center + 3;
-        cmin = co[cminp];
-        for (int i = 1; i < 11; ++i)
-            if (px < W - 3 - 2 * i) {
-                const int t = center + 3 + 2 * i;
-                const float v = co[t];
-                if (cmin < v) {
-                    cmin = v;
-                    cminp = t;
-                }
-            }
-        pos[7] = cminp;
-    }
-    // near neighbours: the first candidate (offset 1) has the other colour,
-    // the V-shaped ones (offset parity even) this colour.
-    if (py > 0) {  // up_near
-        flags |= 1u << 0;
-        cminp = center - W;
-        cmin = co[cminp];
-        csame = false;
-        for (int i = 0; i < 3; ++i) {
-            if (py > 1 + i && px > i) {
-                const int t = center - W - (1 + i) * W - i;
-                const float v = cs[t];
-                if (v < cmin) {
-                    cmin = v;
-                    cminp = t;
-                    csame = true;
-                }
-            }
-            if (py > 1 + i && px < W - 1 - i) {
-                const int t = center - W - (1 + i) * W + i;
-                const float v = cs[t];
-                if (v < cmin) {
-                    cmin = v;
-                    cminp = t;
-                    csame = true;
-                }
-            }
-        }
-        pos[0] = cminp;
-        if (csame) fromsame |= 1u << 0;
-    }
-    if (py < H - 1) {  // down_near
-        flags |= 1u << 2;
-        cminp = center + W;
-        cmin = co[cminp];
-        csame = false;
-        for (int i = 0; i < 3; ++i) {
-            if (py < H - 2 - i && px > i) {
-                const int t = center + W + (1 + i) * W - i;
-                const float v = cs[t];
-                if (v < cmin) {
-                    cmin = v;
-                    cminp = t;
-                    csame = true;
-                }
-            }
-            if (py < H - 2 - i && px < W - 1 - i) {
-                const int t = center + W + (1 + i) * W + i;
-                const float v = cs[t];
-                if (v < cmin) {
-                    cmin = v;
-                    cminp = t;
-                    csame = true;
-                }
-            }
-        }
-        pos[2] = cminp;
-        if (csame) fromsame |= 1u << 2;
-    }
-    if (px > 0) {  // left_near
-        flags |= 1u << 4;
-        cminp = center - 1;
-        cmin = co[cminp];
-        csame = false;
-        for (int i = 0; i < 3; ++i) {
-            if (px > 1 + i && py > i) {
-                const int t = center - 1 - (1 + i) - i * W;
-                const float v = cs[t];
-                if (v < cmin) {
-                    cmin = v;
-                    cminp = t;
-                    csame = true;
-                }
-            }
-            if (px > 1 + i && py < H - 1 - i) {
-                const int t = center - 1 - (1 + i) + i * W;
-                const float v = cs[t];
-                if (v < cmin) {
-                    cmin = v;
-                    cminp = t;
-                    csame = true;
-                }
-            }
-        }
-        pos[4] = cminp;
-        if (csame) fromsame |= 1u << 4;
-    }
-    if (px < W - 1) {  // right_near
-        flags |= 1u << 6;
-        cminp = center + 1;
-        cmin = co[cminp];
-        csame = false;
-        for (int i = 0; i < 3; ++i) {
-            if (px < W - 2 - i && py > i) {
-                const int t = center + 1 + (1 + i) - i * W;
-                const float v = cs[t];
-                if (v < cmin) {
-                    cmin = v;
-                    cminp = t;
-                    csame = true;
-                }
-            }
-            if (px < W - 2 - i && py < H - 1 - i) {
-                const int t = center + 1 + (1 + i) + i * W;
-                const float v = cs[t];
-                if (v < cmin) {
-                    cmin = v;
-                    cminp = t;
-                    csame = true;
-                }
-            }
-        }
-        pos[6] = cminp;
-        if (csame) fromsame |= 1u << 6;
-    }
-
-    // cost matrix; rows of out-of-image neighbours keep the reference's
-    // `float cost_array[8][32] = {2.0f}` contents (2 at [0][0], else 0).
-    float4 npl[8];
-    for (int k = 0; k < 8; ++k) {
-        if (flags & (1u << k)) {
-            const float4* src = V.plane[(fromsame >> k) & 1u ? same : opp];
-            npl[k] = src[pos[k]];
-            const Hyp h = make_hyp(rc, npl[k]);
-            for (int i = 0; i < N; ++i) CA(k, i) = ncc_cost<S, NS>(V, prm, i, h, P, px, py);
-        } else {
-            npl[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-            for (int i = 0; i < N; ++i) CA(k, i) = (k == 0 && i == 0) ? 2.0f : 0.0f;
-        }
-    }
-
-    // multi-hypothesis joint view selection (patch_match_kernel.cu:1114-1176)
-    const uint32_t* so = V.sel[opp];
-    const uint32_t nb_sel[4] = {(flags & 1u) ? so[center - W] : 0u, (flags & 4u) ? so[center + W] : 0u,
-                                (flags & 16u) ? so[center - 1] : 0u, (flags & 64u) ? so[center + 1] : 0u};
-    const float thr = prm.cost_thr[iter];
-    const float fallback = pmath::expf_(thr * thr / (-0.32f));
-    float prob_sum = 0.0f;
-    for (int i = 0; i < N; ++i) {
-        float pri = 0.0f;
-        for (int q = 0; q < 4; ++q)
-            if (flags & (1u << (2 * q))) pri += ((nb_sel[q] >> i) & 1u) ? 0.9f : 0.1f;
-        float count = 0.0f, tmpw = 0.0f;
-        int count_false = 0;
-        for (int k = 0; k < 8; ++k) {
-            const float c = CA(k, i);
-            if (c < thr) {
-                tmpw += pmath::expf_(c * c / (-0.18f));
-                count++;
-            }
-            if (c > 1.2f) count_false++;
-        }
-        float prob = 0.0f;
-        if (count > 2 && count_false < 3)
-            prob = tmpw / count;
-        else if (count_false < 3)
-            prob = fallback;
-        prob = prob * pri;
-        VW(i) = prob;  // PDF held in the weight slots until the draws
-        prob_sum += prob;
-    }
-    {  // TransformPDFToCDF (patch_match_kernel.cu:70-83) then 15 draws
-        const float inv = 1.0f / prob_sum;
-        float cum = 0.0f;
-        for (int i = 0; i < N; ++i) {
-            cum += VW(i) * inv;
-            VW(i) = cum;
-        }
-    }
-    // 15 draws; hits per view (at most 15) are counted in 4-bit fields
-    unsigned long long cnt4[2] = {0ull, 0ull};
-    for (int s = 0; s < 15; ++s) {
-        const float rp = rng.uniform() - 1.1920928955078125e-07f;  // curand_uniform - FLT_EPSILON
-        for (int v = 0; v < N; ++v)
-            if (VW(v) > rp) {
-                cnt4[v >> 4] += 1ull << ((v & 15) * 4);
-                break;
-            }
-    }
-    uint32_t temp_sel = 0;
-    float weight_norm = 0.0f;
-    for (int i = 0; i < N; ++i) {
-        const float w = (float)((cnt4[i >> 4] >> ((i & 15) * 4)) & 15ull);
-        VW(i) = w;
-        if (w > 0) {
-            temp_sel |= 1u << i;
-            weight_norm += w;
-        }
-    }
-
-    // final costs of the 8 candidates (patch_match_kernel.cu:1178-1211;
-    // gmvs/src/patch_match.cu:920-946)
-    float fc[8];
-    for (int k = 0; k < 8; ++k) {
-        float acc = 0.0f;
-        const bool fk = (flags >> k) & 1u;
-        for (int j = 0; j < N; ++j) {
-            const float w = VW(j);
-            if (w > 0) {
-                if (geom && fk)
-                    acc += w * (CA(k, j) + 0.1f * geom_cost(V, j, npl[k], px, py));
-                else
-                    acc += w * CA(k, j);
-            }
-        }
-        fc[k] = acc / weight_norm;
-    }
-    const int min_idx = find_min_idx8(fc);
-
-    // current hypothesis (views with zero weight add +0 in the reference)
-    float4 cur = V.plane[same][center];
-    float cost_now = 0.0f;
     {
-        const Hyp h = make_hyp(rc, cur);
-        for (int i = 0; i < N; ++i) {
-            const float w = VW(i);
-            if (w > 0) {
-                const float c = ncc_cost<S, NS>(V, prm, i, h, P, px, py);
-                if (geom)
-                    cost_now += w * (c + 0.1f * geom_cost(V, i, cur, px, py));
-                else
-                    cost_now += w * c;
+        float cmin;
+        int cminp;
+        bool csame;
+        if (py > 2) {  // up_far (odd offsets only)
+            flags |= 1u << 1;
+            cminp = center - 3 * W;
+            cmin = co[cminp];
+            for (int i = 1; i < 11; ++i)
+                if (py > 2 + 2 * i) {
+                    const int t = center - 3 * W - 2 * i * W;
+                    const float v = co[t];
+                    if (v < cmin) {
+                        cmin = v;
+                        cminp = t;
+                    }
+                }
+            pos[1] = cminp;
+        }
+        if (py < H - 3) {  // down_far
+            flags |= 1u << 3;
+            cminp = center + 3 * W;
+            cmin = co[cminp];
+            for (int i = 1; i < 11; ++i)
+                if (py < H - 3 - 2 * i) {
+                    const int t = center + 3 * W + 2 * i * W;
+                    const float v = co[t];
+                    if (v < cmin) {
+                        cmin = v;
+                        cminp = t;
+                    }
+                }
+            pos[3] = cminp;
+        }
+        if (px > 2) {  // left_far
+            flags |= 1u << 5;
+            cminp = center - 3;
+            cmin = co[cminp];
+            for (int i = 1; i < 11; ++i)
+                if (px > 2 + 2 * i) {
+                    const int t = center - 3 - 2 * i;
+                    const float v = co[t];
+                    if (v < cmin) {
+                        cmin = v;
+                        cminp = t;
+                    }
+                }
+            pos[5] = cminp;
+        }
+        if (px < W - 3) {  // right_far keeps the maximum (patch_match_kernel.cu:954)
+            flags |= 1u << 7;
+            cminp = center + 3;
+            cmin = co[cminp];
+            for (int i = 1; i < 11; ++i)
+                if (px < W - 3 - 2 * i) {
+                    const int t = center + 3 + 2 * i;
+                    const float v = co[t];
+                    if (cmin < v) {
+                        cmin = v;
+                        cminp = t;
+                    }
+                }
+            pos[7] = cminp;
+        }
+        // near neighbours: the first candidate (offset 1) has the other
+        // colour, the V-shaped ones (offset parity even) this colour.
+        if (py > 0) {  // up_near
+            flags |= 1u << 0;
+            cminp = center - W;
+            cmin = co[cminp];
+            csame = false;
+            for (int i = 0; i < 3; ++i) {
+                if (py > 1 + i && px > i) {
+                    const int t = center - W - (1 + i) * W - i;
+                    const float v = cs[t];
+                    if (v < cmin) {
+                        cmin = v;
+                        cminp = t;
+                        csame = true;
+                    }
+                }
+                if (py > 1 + i && px < W - 1 - i) {
+                    const int t = center - W - (1 + i) * W + i;
+                    const float v = cs[t];
+                    if (v < cmin) {
+                        cmin = v;
+                        cminp = t;
+                        csame = true;
+                    }
+                }
             }
+            pos[0] = cminp;
+            if (csame) fromsame |= 1u << 0;
+        }
+        if (py < H - 1) {  // down_near
+            flags |= 1u << 2;
+            cminp = center + W;
+            cmin = co[cminp];
+            csame = false;
+            for (int i = 0; i < 3; ++i) {
+                if (py < H - 2 - i && px > i) {
+                    const int t = center + W + (1 + i) * W - i;
+                    const float v = cs[t];
+                    if (v < cmin) {
+                        cmin = v;
+                        cminp = t;
+                        csame = true;
+                    }
+                }
+                if (py < H - 2 - i && px < W - 1 - i) {
+                    const int t = center + W + (1 + i) * W + i;
+                    const float v = cs[t];
+                    if (v < cmin) {
+                        cmin = v;
+                        cminp = t;
+                        csame = true;
+                    }
+                }
+            }
+            pos[2] = cminp;
+            if (csame) fromsame |= 1u << 2;
+        }
+        if (px > 0) {  // left_near
+            flags |= 1u << 4;
+            cminp = center - 1;
+            cmin = co[cminp];
+            csame = false;
+            for (int i = 0; i < 3; ++i) {
+                if (px > 1 + i && py > i) {
+                    const int t = center - 1 - (1 + i) - i * W;
+                    const float v = cs[t];
+                    if (v < cmin) {
+                        cmin = v;
+                        cminp = t;
+                        csame = true;
+                    }
+                }
+                if (px > 1 + i && py < H - 1 - i) {
+                    const int t = center - 1 - (1 + i) + i * W;
+                    const float v = cs[t];
+                    if (v < cmin) {
+                        cmin = v;
+                        cminp = t;
+                        csame = true;
+                    }
+                }
+            }
+            pos[4] = cminp;
+            if (csame) fromsame |= 1u << 4;
+        }
+        if (px < W - 1) {  // right_near
+            flags |= 1u << 6;
+            cminp = center + 1;
+            cmin = co[cminp];
+            csame = false;
+            for (int i = 0; i < 3; ++i) {
+                if (px < W - 2 - i && py > i) {
+                    const int t = center + 1 + (1 + i) - i * W;
+                    const float v = cs[t];
+                    if (v < cmin) {
+                        cmin = v;
+                        cminp = t;
+                        csame = true;
+                    }
+                }
+                if (px < W - 2 - i && py < H - 1 - i) {
+                    const int t = center + 1 + (1 + i) + i * W;
+                    const float v = cs[t];
+                    if (v < cmin) {
+                        cmin = v;
+                        cminp = t;
+                        csame = true;
+                    }
+                }
+            }
+            pos[6] = cminp;
+            if (csame) fromsame |= 1u << 6;
         }
     }
-    cost_now /= weight_norm;
-    float cur_cost = cost_now;
-    uint32_t cur_sel = V.sel[same][center];
-    float depth_now = depth_from_plane(rc, cur, px, py);
-    float restricted_cost = 0.0f;
+    for (int k = 0; k < 8; ++k)
+        if ((flags >> k) & 1u) POS(k) = pos[k];
+#define NPL(k) (V.plane[((fromsame >> (k)) & 1u) ? same : opp][POS(k)])
+
+    // state carried between the phases of the hypothesis loop
+    float weight_norm = 0.0f, cost_now = 0.0f, cur_cost = 0.0f, depth_now = 0.0f, restricted_cost = 0.0f;
+    float depth_prior = 0.0f, depth_rand = 0.0f, dnow = 0.0f, depth_pert = 0.0f;
+    uint32_t temp_sel = 0u, cur_sel = V.sel[same][center];
+    float4 cur = V.plane[same][center];
+    float4 ppl = make_float4(0.f, 0.f, 0.f, 0.f);
     const PriorK pk = prior_k(V);
     const uint32_t mask = prior_mode ? V.prior_masks[center] : 0u;
-    float4 ppl = make_float4(0.f, 0.f, 0.f, 0.f);
-    float depth_prior = 0.0f;
+    const bool use_prior = prior_mode && mask > 0;
+    int min_idx = 0;
 
-    if (prior_mode) {
-        ppl = V.prior_planes[center];
-        depth_prior = depth_from_plane(rc, ppl, px, py);
-        if (mask > 0) {
-            float rfc[8];
-            for (int k = 0; k < 8; ++k) {
-                rfc[k] = 0.0f;
-                if ((flags >> k) & 1u) {
-                    const float4 q = npl[k];
-                    const float dn = depth_from_plane(rc, q, px, py);
-                    const float ac = ppl.x * q.x + ppl.y * q.y + ppl.z * q.z;
-                    rfc[k] = restricted(pk, fc[k], dn - depth_prior, ac);
+    for (int s = 0; s < 14; ++s) {
+        float4 pl;
+        const bool all_views = s < 8;
+        if (s < 8) {
+            if (!((flags >> s) & 1u)) {
+                // the reference's `float cost_array[8][32] = {2.0f}` (2 at [0][0], else 0)
+                for (int i = 0; i < N; ++i) CA(s, i) = (s == 0 && i == 0) ? 2.0f : 0.0f;
+                continue;
+            }
+            pl = NPL(s);
+        } else if (s == 8) {
+            // multi-hypothesis joint view selection (patch_match_kernel.cu:1114-1176)
+            const uint32_t* so = V.sel[opp];
+            const uint32_t nb_sel[4] = {(flags & 1u) ? so[center - W] : 0u, (flags & 4u) ? so[center + W] : 0u,
+                                        (flags & 16u) ? so[center - 1] : 0u, (flags & 64u) ? so[center + 1] : 0u};
+            const float thr = prm.cost_thr[iter];
+            const float fallback = pmath::expf_(thr * thr / (-0.32f));
+            float prob_sum = 0.0f;
+            for (int i = 0; i < N; ++i) {
+                float pri = 0.0f;
+                for (int k = 0; k < 4; ++k)
+                    if (flags & (1u << (2 * k))) pri += ((nb_sel[k] >> i) & 1u) ? 0.9f : 0.1f;
+                float count = 0.0f, tmpw = 0.0f;
+                int count_false = 0;
+                for (int k = 0; k < 8; ++k) {
+                    const float c = CA(k, i);
+                    if (c < thr) {
+                        tmpw += pmath::expf_(c * c / (-0.18f));
+                        count++;
+                    }
+                    if (c > 1.2f) count_false++;
+                }
+                float prob = 0.0f;
+                if (count > 2 && count_false < 3)
+                    prob = tmpw / count;
+                else if (count_false < 3)
+                    prob = fallback;
+                prob = prob * pri;
+                VW(i) = prob;  // the PDF lives in the weight slots until the draws
+                prob_sum += prob;
+            }
+            {  // TransformPDFToCDF (patch_match_kernel.cu:70-83)
+                const float inv = 1.0f / prob_sum;
+                float cum = 0.0f;
+                for (int i = 0; i < N; ++i) {
+                    cum += VW(i) * inv;
+                    VW(i) = cum;
                 }
             }
-            const int max_idx = find_max_idx8(rfc);
-            const float dn = depth_from_plane(rc, cur, px, py);
-            const float ac = ppl.x * cur.x + ppl.y * cur.y + ppl.z * cur.z;
-            const float rcn = restricted(pk, cost_now, dn - depth_prior, ac);
-            if ((flags >> max_idx) & 1u) {
-                const float4 q = npl[max_idx];
-                const float db = depth_from_plane(rc, q, px, py);
-                if (db >= V.depth_min && db <= V.depth_max && rfc[max_idx] > rcn) {
-                    depth_now = db;
-                    cur = q;
-                    cur_cost = fc[max_idx];
-                    restricted_cost = rfc[max_idx];
-                    cur_sel = temp_sel;
-                }
+            // 15 draws; hits per view (at most 15) counted in 4-bit fields
+            unsigned long long cnt4[2] = {0ull, 0ull};
+            for (int d = 0; d < 15; ++d) {
+                const float rp = rng.uniform() - 1.1920928955078125e-07f;  // curand_uniform - FLT_EPSILON
+                for (int v = 0; v < N; ++v)
+                    if (VW(v) > rp) {
+                        cnt4[v >> 4] += 1ull << ((v & 15) * 4);
+                        break;
+                    }
             }
-        } else if ((flags >> min_idx) & 1u) {  // no selected-view update (patch_match_kernel.cu:1306-1318)
-            const float4 q = npl[min_idx];
-            const float db = depth_from_plane(rc, q, px, py);
-            if (db >= V.depth_min && db <= V.depth_max && fc[min_idx] < cost_now) {
-                depth_now = db;
-                cur = q;
-                cur_cost = fc[min_idx];
-            }
-        }
-    } else if ((flags >> min_idx) & 1u) {
-        const float4 q = npl[min_idx];
-        const float db = depth_from_plane(rc, q, px, py);
-        if (db >= V.depth_min && db <= V.depth_max && fc[min_idx] < cost_now) {
-            depth_now = db;
-            cur = q;
-            cur_cost = fc[min_idx];
-            cur_sel = temp_sel;
-        }
-    }
-
-    // PlaneHypothesisRefinement (patch_match_kernel.cu:684-811)
-    {
-        const float pert = 0.02f;
-        const bool use_prior = prior_mode && mask > 0;
-        float depth_rand;
-        float4 n_rand;
-        if (use_prior) {
-            depth_rand = rng.uniform() * 6 * pk.depth_sigma + (depth_prior - 3 * pk.depth_sigma);
-            n_rand = perturbed_normal(rc, px, py, ppl, rng, pk.angle_sigma);
-        } else {
-            depth_rand = rng.uniform() * (V.depth_max - V.depth_min) + V.depth_min;
-            n_rand = random_normal(rc, px, py, rng, depth_now);
-        }
-        const float dmin_p = (1 - pert) * depth_now;
-        const float dmax_p = (1 + pert) * depth_now;
-        const float depth_pert = rng.uniform() * (dmax_p - dmin_p) + dmin_p;
-        const float4 n_pert = perturbed_normal(rc, px, py, cur, rng, (float)(pert * 3.14159265358979323846));
-        const float4 base = cur;
-        const float dnow = depth_now;
-        for (int k = 0; k < 5; ++k) {
-            float4 cand;
-            float dk;
-            switch (k) {
-                case 0: cand = base; dk = depth_rand; break;
-                case 1: cand = n_rand; dk = dnow; break;
-                case 2: cand = n_rand; dk = depth_rand; break;
-                case 3: cand = n_pert; dk = dnow; break;
-                default: cand = base; dk = depth_pert; break;
-            }
-            cand.w = distance_to_origin(rc, px, py, dk, cand);
-            const Hyp h = make_hyp(rc, cand);
-            float tc = 0.0f;
-            for (int j = 0; j < N; ++j) {
-                const float w = VW(j);
+            for (int i = 0; i < N; ++i) {
+                const float w = (float)((cnt4[i >> 4] >> ((i & 15) * 4)) & 15ull);
+                VW(i) = w;
                 if (w > 0) {
-                    const float c = ncc_cost<S, NS>(V, prm, j, h, P, px, py);
-                    if (geom)
-                        tc += w * (c + 0.1f * geom_cost(V, j, cand, px, py));
-                    else
-                        tc += w * c;
+                    temp_sel |= 1u << i;
+                    weight_norm += w;
                 }
             }
-            tc /= weight_norm;
-            const float db = depth_from_plane(rc, cand, px, py);
+            // final costs of the 8 candidates (patch_match_kernel.cu:1178-1211;
+            // gmvs/src/patch_match.cu:920-946)
+            for (int k = 0; k < 8; ++k) {
+                float acc = 0.0f;
+                const bool fk = (flags >> k) & 1u;
+                for (int j = 0; j < N; ++j) {
+                    const float w = VW(j);
+                    if (w > 0) {
+                        if (geom && fk)
+                            acc += w * (CA(k, j) + 0.1f * geom_cost(V, j, NPL(k), px, py));
+                        else
+                            acc += w * CA(k, j);
+                    }
+                }
+                FC(k) = acc / weight_norm;
+            }
+            {  // FindMinCostIndex: ties pick the last index
+                float m = FC(0);
+                for (int k = 1; k < 8; ++k)
+                    if (FC(k) <= m) {
+                        m = FC(k);
+                        min_idx = k;
+                    }
+            }
+            pl = cur;
+        } else {
+            if (s == 9) {
+                cur_cost = cost_now;
+                depth_now = depth_from_plane(rc, cur, px, py);
+                if (prior_mode) {
+                    ppl = V.prior_planes[center];
+                    depth_prior = depth_from_plane(rc, ppl, px, py);
+                    if (mask > 0) {  // patch_match_kernel.cu:1256-1305
+                        float rfc[8];
+                        for (int k = 0; k < 8; ++k) {
+                            rfc[k] = 0.0f;
+                            if ((flags >> k) & 1u) {
+                                const float4 qp = NPL(k);
+                                const float dn = depth_from_plane(rc, qp, px, py);
+                                const float ac = ppl.x * qp.x + ppl.y * qp.y + ppl.z * qp.z;
+                                rfc[k] = restricted(pk, FC(k), dn - depth_prior, ac);
+                            }
+                        }
+                        const int max_idx = find_max_idx8(rfc);
+                        const float dn = depth_from_plane(rc, cur, px, py);
+                        const float ac = ppl.x * cur.x + ppl.y * cur.y + ppl.z * cur.z;
+                        const float rcn = restricted(pk, cost_now, dn - depth_prior, ac);
+                        if ((flags >> max_idx) & 1u) {
+                            const float4 qp = NPL(max_idx);
+                            const float db = depth_from_plane(rc, qp, px, py);
+                            if (db >= V.depth_min && db <= V.depth_max && rfc[max_idx] > rcn) {
+                                depth_now = db;
+                                cur = qp;
+                                cur_cost = FC(max_idx);
+                                restricted_cost = rfc[max_idx];
+                                cur_sel = temp_sel;
+                            }
+                        }
+                    } else if ((flags >> min_idx) & 1u) {  // no selected-view update (1306-1318)
+                        const float4 qp = NPL(min_idx);
+                        const float db = depth_from_plane(rc, qp, px, py);
+                        if (db >= V.depth_min && db <= V.depth_max && FC(min_idx) < cost_now) {
+                            depth_now = db;
+                            cur = qp;
+                            cur_cost = FC(min_idx);
+                        }
+                    }
+                } else if ((flags >> min_idx) & 1u) {
+                    const float4 qp = NPL(min_idx);
+                    const float db = depth_from_plane(rc, qp, px, py);
+                    if (db >= V.depth_min && db <= V.depth_max && FC(min_idx) < cost_now) {
+                        depth_now = db;
+                        cur = qp;
+                        cur_cost = FC(min_idx);
+                        cur_sel = temp_sel;
+                    }
+                }
+                // refinement candidates (patch_match_kernel.cu:684-760)
+                const float pert = 0.02f;
+                float4 n_rand;
+                if (use_prior) {
+                    depth_rand = rng.uniform() * 6 * pk.depth_sigma + (depth_prior - 3 * pk.depth_sigma);
+                    n_rand = perturbed_normal(rc, px, py, ppl, rng, pk.angle_sigma);
+                } else {
+                    depth_rand = rng.uniform() * (V.depth_max - V.depth_min) + V.depth_min;
+                    n_rand = random_normal(rc, px, py, rng, depth_now);
+                }
+                const float dmin_p = (1 - pert) * depth_now;
+                const float dmax_p = (1 + pert) * depth_now;
+                depth_pert = rng.uniform() * (dmax_p - dmin_p) + dmin_p;  // do/while runs once (quirk)
+                const float4 n_pert = perturbed_normal(rc, px, py, cur, rng, (float)(pert * 3.14159265358979323846));
+                // slots: 0 = base plane (after propagation), 1 = random normal, 2 = perturbed normal
+                PL4(0, 0) = cur.x, PL4(0, 1) = cur.y, PL4(0, 2) = cur.z, PL4(0, 3) = cur.w;
+                PL4(1, 0) = n_rand.x, PL4(1, 1) = n_rand.y, PL4(1, 2) = n_rand.z, PL4(1, 3) = n_rand.w;
+                PL4(2, 0) = n_pert.x, PL4(2, 1) = n_pert.y, PL4(2, 2) = n_pert.z, PL4(2, 3) = n_pert.w;
+                dnow = depth_now;
+            }
+            // candidates (depth, normal): (rand, base), (now, rand), (rand, rand), (now, pert), (pert, base)
+            const int k = s - 9;
+            const int slot = (k == 1 || k == 2) ? 1 : (k == 3 ? 2 : 0);
+            const float dk = (k == 0 || k == 2) ? depth_rand : (k == 4 ? depth_pert : dnow);
+            pl = make_float4(PL4(slot, 0), PL4(slot, 1), PL4(slot, 2), PL4(slot, 3));
+            pl.w = distance_to_origin(rc, px, py, dk, pl);
+        }
+
+        // the hypothesis against every source view (neighbours) or the
+        // sampled ones (current plane, refinement)
+        const Hyp hy = make_hyp(rc, pl);
+        float acc = 0.0f;
+        for (int j = 0; j < N; ++j) {
+            float w = 0.0f;
+            if (!all_views) {
+                w = VW(j);
+                if (!(w > 0)) continue;
+            }
+            const float c = ncc_cost<S, NS>(V, prm, j, hy, P, px, py, q);
+            if (all_views)
+                CA(s, j) = c;
+            else if (geom)
+                acc += w * (c + 0.1f * geom_cost(V, j, pl, px, py));
+            else
+                acc += w * c;
+        }
+        if (s == 8) {
+            cost_now = acc / weight_norm;
+        } else if (s > 8) {
+            const float tc = acc / weight_norm;
+            const float db = depth_from_plane(rc, pl, px, py);
+            const float dk = (s == 9 || s == 11) ? depth_rand : ((s == 13) ? depth_pert : dnow);
             if (use_prior) {
-                const float ac = ppl.x * cand.x + ppl.y * cand.y + ppl.z * cand.z;
+                const float ac = ppl.x * pl.x + ppl.y * pl.y + ppl.z * pl.z;
                 const float rtc = restricted(pk, tc, dk - depth_prior, ac);
                 if (db >= V.depth_min && db <= V.depth_max && rtc > restricted_cost) {
                     depth_now = db;
-                    cur = cand;
+                    cur = pl;
                     cur_cost = tc;
                     restricted_cost = rtc;
                 }
             } else if (db >= V.depth_min && db <= V.depth_max && tc < cur_cost) {
                 depth_now = db;
-                cur = cand;
+                cur = pl;
                 cur_cost = tc;
             }
         }
     }
-    V.plane[outb][center] = cur;
-    V.cost[outb][center] = cur_cost;
-    V.sel[outb][center] = cur_sel;
+    if (q.h == 0) {
+        V.plane[outb][center] = cur;
+        V.cost[outb][center] = cur_cost;
+        V.sel[outb][center] = cur_sel;
+    }
+#undef NPL
+#undef PL4
+#undef FC
+#undef POS
 #undef CA
 #undef VW
 }

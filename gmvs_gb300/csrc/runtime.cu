@@ -172,7 +172,8 @@ size_t bytes_per_pixel(int variant) {
     }
 }
 
-int tile_w_of(const gmvs_params*) { return 32; }
+// a tile is 16 pixel columns (one lane pair per pixel in the PatchMatch kernels)
+int tile_w_of(const gmvs_params*) { return 16; }
 int tile_h_of(const gmvs_params* p) { return p->tile_h > 0 ? p->tile_h : 4; }
 
 int num_offsets(const gmvs_params* p) {
@@ -507,10 +508,10 @@ int32_t build_plan(gmvs_plan* P, const gmvs_view_pass* views, int32_t n, const g
         e = cudaMemcpyAsync(P->d_tiles, ht.data(), sizeof(Tile) * ht.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host vectors die at return
     if (e != cudaSuccess) return fail_cuda(e, "uploading plan descriptors");
-    const int nthr = TW * TH;
+    const int npix = TW * TH;
     const int grid = std::max(1, std::min(L.ntiles, num_sms() * 16));
-    P->init_ls = LaunchShape{grid, dim3(TW, TH), (size_t)2 * nmax * nthr * 4};
-    P->sweep_ls = LaunchShape{grid, dim3(TW, TH), (size_t)9 * nmax * nthr * 4};
+    P->init_ls = LaunchShape{grid, dim3(2 * TW, TH), (size_t)2 * nmax * npix * 4};
+    P->sweep_ls = LaunchShape{grid, dim3(2 * TW, TH), (size_t)(9 * nmax + 28) * npix * 4};
     P->fin_ls = LaunchShape{grid, dim3(TW, TH), 0};
     P->num_stages = 2 * p->max_iterations + 4;
     P->final_buf = p->max_iterations & 1;

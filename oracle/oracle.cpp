@@ -16,8 +16,9 @@
 // with the CUDA kernels so both round identically: the homography is
 // H = A - b g^T with A = K_s R_rel K_r^-1 and b = K_s t_rel formed in FP64
 // and rounded once, projected coordinates are X * (1 / Z) with a correctly
-// rounded reciprocal, every fused multiply-add is explicit (std::fma), the
-// window moments are summed sequentially, and exp / sin / cos / acos come
+// rounded reciprocal, every fused multiply-add is explicit (std::fma), each
+// window moment is (left half of the columns) + (right half), and
+// exp / sin / cos / acos come
 // from gmvs_gb300/csrc/pmath.h.  The reference chains the same algebra in
 // fp32 (ComputeHomography, patch_match_kernel.cu:262-360); the fp64 path
 // below restates that chain in double and serves as the FP64 oracle.
@@ -355,31 +356,38 @@ inline T bilinear_clamp(const float* img, T u, T v, int H, int W) {
 }
 // Module A tex2D<float>(tex, x, y) on a float32 texture with
 // cudaFilterModeLinear, unnormalised coordinates (planar_initer.cu:150-158):
-// x_B = x - 0.5, i = floor(x_B), alpha = frac(x_B) held with 8 fractional
-// bits, rounded half up; out-of-range texel indices are clamped to the edge
-// (cudaAddressModeWrap acts as clamp with unnormalised coordinates).  Pinned
-// on a GB300 against 2600 hardware fetches (fraction sweeps in x and y,
-// ties, out-of-range coordinates): all equal bit for bit.
+// x_B = x - 0.5, i = floor(x_B); the fractions a, b are held with 8
+// fractional bits, rounded half up; the corner weight w11 = a*b is rounded
+// half up to 8 fractional bits and the other weights follow from it
+// (a - w11, b - w11, 1 - a - b + w11); out-of-range texel indices are
+// clamped to the edge (cudaAddressModeWrap acts as clamp with unnormalised
+// coordinates).  Pinned on a GB300 against 42,600 hardware fetches
+// (fraction sweeps, ties, random full-precision coordinates inside and
+// outside the texture): all equal bit for bit.  The fp64 path is the ideal
+// (unquantised) bilinear interpolation.
 template <class T>
 inline T tex2d_linear(const float* img, float x, float y, int H, int W) {
     const float xb = x - 0.5f, yb = y - 0.5f;
     const float fx = std::floor(xb), fy = std::floor(yb);
     if (!(fx == fx) || !(fy == fy)) return (T)NAN;
-    T a, b;
-    if (std::is_same<T, double>::value) {
-        a = (T)xb - (T)fx;
-        b = (T)yb - (T)fy;
+    double a, b, w00, w10, w01, w11;
+    a = (double)xb - (double)fx;
+    b = (double)yb - (double)fy;
+    if (!std::is_same<T, double>::value) {
+        a = std::floor(a * 256.0 + 0.5) / 256.0;
+        b = std::floor(b * 256.0 + 0.5) / 256.0;
+        w11 = std::floor(a * b * 256.0 + 0.5) / 256.0;
     } else {
-        a = (T)(std::floor(((double)xb - (double)fx) * 256.0 + 0.5) / 256.0);
-        b = (T)(std::floor(((double)yb - (double)fy) * 256.0 + 0.5) / 256.0);
+        w11 = a * b;
     }
+    w10 = a - w11;
+    w01 = b - w11;
+    w00 = 1.0 - a - b + w11;
     const double ix = clampv((double)fx, -1.0, (double)W), iy = clampv((double)fy, -1.0, (double)H);
     const int i0 = clampv((int)ix, 0, W - 1), i1 = clampv((int)ix + 1, 0, W - 1);
     const int j0 = clampv((int)iy, 0, H - 1), j1 = clampv((int)iy + 1, 0, H - 1);
-    const T t00 = img[j0 * W + i0], t10 = img[j0 * W + i1];
-    const T t01 = img[j1 * W + i0], t11 = img[j1 * W + i1];
-    const T one = (T)1;
-    return (one - a) * (one - b) * t00 + a * (one - b) * t10 + (one - a) * b * t01 + a * b * t11;
+    const double v = w00 * img[j0 * W + i0] + w10 * img[j0 * W + i1] + w01 * img[j1 * W + i0] + w11 * img[j1 * W + i1];
+    return (T)v;
 }
 
 // ----------------------------------------------------------------- views --
@@ -531,7 +539,9 @@ T bilateral_ncc(const ViewSet& vs, int src, int px, int py, const F4& pl) {
 // ComputeBilateralNCC in the shared fp32 formulation (see the file header):
 // module A (patch_match_kernel.cu:412-516) or module B (patch_match.cu:
 // 347-445) sampling, H = A - b g^T, X * (1 / Z), explicit fused
-// multiply-adds, sequential window sums in (x offset, y offset) order.
+// multiply-adds; each window sum is accumulated over the left half of the
+// window columns and over the right half in (x offset, y offset) order, and
+// the two halves are added.
 inline float ncc_f32(const ViewSet& vs, int src, int px, int py, const F4& pl) {
     const Cam& rc = vs.cams[0];
     const Cam& sc = vs.cams[src];
@@ -553,8 +563,13 @@ inline float ncc_f32(const ViewSet& vs, int src, int px, int py, const F4& pl) {
     const float* sim = vs.img(src);
     const bool tex = vs.sampler == 1;
     const float center = tex ? tex2d_linear<float>(ref, fpx + 0.5f, fpy + 0.5f, Hh, Ww) : ref[py * Ww + px];
-    float s_w = 0.f, s_r = 0.f, s_rr = 0.f, ss = 0.f, sss = 0.f, srs = 0.f;
-    for (int i = -radius; i < radius + 1; i += vs.radius_increment) {
+    // window sums: left half of the columns (x offsets) + right half
+    const int ncol = (2 * radius) / vs.radius_increment + 1;
+    const int half = (ncol + 1) / 2;
+    float acc[2][6] = {{0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}};
+    for (int ci = 0; ci < ncol; ++ci) {
+        const int i = -radius + ci * vs.radius_increment;
+        float* A = acc[ci < half ? 0 : 1];  // s_w, s_r, s_rr, ss, sss, srs
         for (int j = -radius; j < radius + 1; j += vs.radius_increment) {
             int qx = px + i, qy = py + j;
             if (!tex) {
@@ -565,9 +580,9 @@ inline float ncc_f32(const ViewSet& vs, int src, int px, int py, const F4& pl) {
                                 : ref[qy * Ww + qx];
             const float w = bilateral_weight<float>((float)i, (float)j, r, center, vs.sigma_spatial, vs.sigma_color);
             const float wr = w * r;
-            s_r += wr;
-            s_rr = std::fma(wr, r, s_rr);
-            s_w += w;
+            A[1] += wr;
+            A[2] = std::fma(wr, r, A[2]);
+            A[0] += w;
             const float fqx = (float)qx, fqy = (float)qy;
             const float bx = std::fma(m[0], fqx, m[2]), by = std::fma(m[3], fqx, m[5]), bz = std::fma(m[6], fqx, m[8]);
             const float rz = 1.0f / std::fma(m[7], fqy, bz);
@@ -576,11 +591,13 @@ inline float ncc_f32(const ViewSet& vs, int src, int px, int py, const F4& pl) {
             const float s = tex ? tex2d_linear<float>(sim, u + 0.5f, v + 0.5f, Hh, Ww)
                                 : bilinear_clamp<float>(sim, u, v, Hh, Ww);
             const float ws = w * s;
-            ss += ws;
-            sss = std::fma(ws, s, sss);
-            srs = std::fma(wr, s, srs);
+            A[3] += ws;
+            A[4] = std::fma(ws, s, A[4]);
+            A[5] = std::fma(wr, s, A[5]);
         }
     }
+    const float s_w = acc[0][0] + acc[1][0], s_r = acc[0][1] + acc[1][1], s_rr = acc[0][2] + acc[1][2];
+    const float ss = acc[0][3] + acc[1][3], sss = acc[0][4] + acc[1][4], srs = acc[0][5] + acc[1][5];
     const float inv = 1.0f / s_w;
     const float mean_r = s_r * inv;
     const float var_r = s_rr * inv - mean_r * mean_r;
