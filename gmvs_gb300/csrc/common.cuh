@@ -31,6 +31,7 @@ struct DevCam {  // world -> camera, as gmvs_camera without the extents
 // A_j and b_j are formed once per view pair in FP64 and rounded once.
 struct DevView {
     int H, W, N, stream_id;
+    int init_kind, sweep_kind, pass_index;  // per view, so one launch can mix passes
     float depth_min, depth_max;
     float src_w[kMaxNgb], src_h[kMaxNgb];  // centre test extents (camera width/height)
     float A[kMaxNgb][9];

@@ -26,11 +26,17 @@ struct SampF32 {  // plain fp32 rows, four loads per sample
 // Texel quads: quad[y][x] = (I[y][x], I[y][xu], I[yu][x], I[yu][xu]) with
 // xu = min(x+1, W-1), yu = min(y+1, H-1), i.e. the four taps the reference
 // reads for a sample whose clamped integer corner is (x, y).
+// hl = clamp(trunc(v), 0, H - 1) exactly as the reference, without int/float
+// conversions: clamping first makes trunc == floor, and adding 2^23 with
+// round-down leaves floor(v) in the low mantissa bits.  NaN -> 0 and +-inf
+// clamp to the edges like the saturating conversion.
 __device__ __forceinline__ void clamp_corner(float u, float v, int H, int W, int& idx, float& wd, float& hd) {
-    const int hl = min(max(__float2int_rz(v), 0), H - 1);
-    const int wl = min(max(__float2int_rz(u), 0), W - 1);
-    hd = v - (float)hl;
-    wd = u - (float)wl;
+    const float vc = fminf(fmaxf(v, 0.0f), (float)(H - 1));
+    const float uc = fminf(fmaxf(u, 0.0f), (float)(W - 1));
+    const float tv = __fadd_rd(vc, 8388608.0f), tu = __fadd_rd(uc, 8388608.0f);
+    const int hl = __float_as_int(tv) - 0x4B000000, wl = __float_as_int(tu) - 0x4B000000;
+    hd = v - (tv - 8388608.0f);
+    wd = u - (tu - 8388608.0f);
     idx = hl * W + wl;
 }
 
@@ -113,11 +119,13 @@ __device__ __forceinline__ Pair make_pair(unsigned lane) { return Pair{(int)(lan
 // left + right: lane 0 adds (l, r), lane 1 adds (r, l); IEEE addition commutes
 __device__ __forceinline__ float pair_sum(const Pair& q, float v) { return v + __shfl_xor_sync(q.mask, v, 1); }
 
+// The per-lane window weights (w, w * I_ref) live in shared memory: slot
+// k of this lane at pw[k * pstride], k = column-in-half * NS + row.
 template <int NS>
 struct Patch {
     static constexpr int NC = NS / 2;  // columns per lane (NS even)
-    float w[NC * NS];
-    float wr[NC * NS];
+    float2* pw;
+    int pstride;
     float inv, mean_r, var_r;
 };
 template <>
@@ -147,7 +155,7 @@ __device__ __forceinline__ void make_patch(Patch<NS>& P, const S& ref, const Dev
     if constexpr (NS > 0) {
         constexpr int NC = NS / 2;
         const float center = ref.at(px, py);
-#pragma unroll
+#pragma unroll 1
         for (int al = 0; al < NC; ++al) {
             const int qx = window_coord<S>(px, -radius + (q.h * NC + al) * inc, V.W);
 #pragma unroll
@@ -156,8 +164,7 @@ __device__ __forceinline__ void make_patch(Patch<NS>& P, const S& ref, const Dev
                 const float w = bilateral_weight((float)(-radius + (q.h * NC + al) * inc), (float)(-radius + b * inc),
                                                  r, center, prm.sigma_spatial, prm.sigma_color);
                 const float wr = w * r;
-                P.w[al * NS + b] = w;
-                P.wr[al * NS + b] = wr;
+                P.pw[(al * NS + b) * P.pstride] = make_float2(w, wr);
                 s_r += wr;
                 s_rr = fmaf(wr, r, s_rr);
                 s_w += w;
@@ -226,21 +233,25 @@ __device__ __forceinline__ float ncc_cost(const DevView& V, const DevParams& prm
         constexpr int NC = NS / 2;
         const int radius = prm.patch_size / 2;
         const int inc = prm.radius_increment;
+        float qys[NS];
 #pragma unroll
+        for (int bb = 0; bb < NS; ++bb) qys[bb] = (float)window_coord<S>(py, -radius + bb * inc, V.H);
+#pragma unroll 1
         for (int al = 0; al < NC; ++al) {
             const float qx = (float)window_coord<S>(px, -radius + (q.h * NC + al) * inc, V.W);
             const float bx = fmaf(m0, qx, m2), by = fmaf(m3, qx, m5), bz = fmaf(m6, qx, m8);
 #pragma unroll
             for (int bb = 0; bb < NS; ++bb) {
-                const float qy = (float)window_coord<S>(py, -radius + bb * inc, V.H);
+                const float qy = qys[bb];
                 const float rz = rcp_rn(fmaf(m7, qy, bz));
                 const float u = fmaf(m1, qy, bx) * rz;
                 const float v = fmaf(m4, qy, by) * rz;
                 const float s = src.sample(u, v);
-                const float ws = P.w[al * NS + bb] * s;
+                const float2 wt = P.pw[(al * NS + bb) * P.pstride];
+                const float ws = wt.x * s;
                 ss += ws;
                 sss = fmaf(ws, s, sss);
-                srs = fmaf(P.wr[al * NS + bb], s, srs);
+                srs = fmaf(wt.y, s, srs);
             }
         }
     } else {
@@ -320,7 +331,7 @@ __device__ __forceinline__ float4 normal_to_cam(const DevCam& c, float4 p) {
 }
 
 // GenerateRandomNormal (patch_match_kernel.cu:137-172); rejection bounded at 64.
-__device__ __forceinline__ float4 random_normal(const DevCam& c, int px, int py, DevRng& rng, float depth) {
+__device__ __noinline__ float4 random_normal(const DevCam& c, int px, int py, DevRng& rng, float depth) {
     float q1 = 1.0f, q2 = 1.0f, s = 2.0f;
     for (int it = 0; it < 64 && s >= 1.0f; ++it) {
         q1 = 2.0f * rng.uniform() - 1.0f;
@@ -345,7 +356,7 @@ __device__ __forceinline__ float4 random_normal(const DevCam& c, int px, int py,
 }
 
 // GeneratePerturbedNormal (patch_match_kernel.cu:174-213)
-__device__ __forceinline__ float4 perturbed_normal(const DevCam& c, int px, int py, float4 n, DevRng& rng, float pert) {
+__device__ __noinline__ float4 perturbed_normal(const DevCam& c, int px, int py, float4 n, DevRng& rng, float pert) {
     const float4 vd = view_direction(c, px, py, 1.0f);
     const float a1 = (rng.uniform() - 0.5f) * pert;
     const float a2 = (rng.uniform() - 0.5f) * pert;
@@ -363,7 +374,7 @@ __device__ __forceinline__ float4 perturbed_normal(const DevCam& c, int px, int 
 }
 
 // compute_geom_consistency_cost (gmvs/src/patch_match.cu:562-593)
-__device__ __forceinline__ float geom_cost(const DevView& V, int j, float4 pl, int px, int py) {
+__device__ __noinline__ float geom_cost(const DevView& V, int j, float4 pl, int px, int py) {
     const DevCam& rc = V.cam[0];
     const DevCam& sc = V.cam[j + 1];
     const float depth = depth_from_plane(rc, pl, px, py);
@@ -395,7 +406,7 @@ __device__ __forceinline__ PriorK prior_k(const DevView& V) {
     k.beta = 0.18f;
     return k;
 }
-__device__ __forceinline__ float restricted(const PriorK& k, float cost, float dd, float ac) {
+__device__ __noinline__ float restricted(const PriorK& k, float cost, float dd, float ac) {
     const float ad = pmath::acosf_(ac);
     const float pr = k.gamma + pmath::expf_(-dd * dd / k.two_dsq) * pmath::expf_(-ad * ad / k.two_asq);
     return pmath::expf_(-cost * cost / k.beta) * pr;
@@ -432,19 +443,19 @@ __device__ __forceinline__ int find_max_idx8(const float* c) {
 // 2 * nmax floats; both lanes write the same values.
 template <class S, int NS>
 __device__ void init_pixel(const DevView& V, const DevParams& prm, int px, int py, float* cv, int npix,
-                           const Pair& q) {
+                           const Pair& q, float2* pw, int pstride) {
     const int W = V.W, N = V.N;
     const int c = py * W + px;
     const DevCam& rc = V.cam[0];
-    DevRng rng(prm.seed_lo, prm.seed_hi, (uint32_t)c, (uint32_t)V.stream_id, phase_of(prm.pass_index, 0));
+    DevRng rng(prm.seed_lo, prm.seed_hi, (uint32_t)c, (uint32_t)V.stream_id, phase_of(V.pass_index, 0));
     float4 pl;
-    if (prm.init_kind == GMVS_INIT_DEPTH_NORMAL) {
+    if (V.init_kind == GMVS_INIT_DEPTH_NORMAL) {
         // compute_plane_hypothesis_from_normal_depth (gmvs/src/patch_match.cu:329-339)
         pl = make_float4(V.ref_normal[c * 3 + 0], V.ref_normal[c * 3 + 1], V.ref_normal[c * 3 + 2], V.dep[0][c]);
         pl = normal_to_cam(rc, pl);
         const float depth = pl.w;
         pl.w = distance_to_origin(rc, px, py, depth, pl);
-    } else if (prm.init_kind == GMVS_INIT_PRIOR) {
+    } else if (V.init_kind == GMVS_INIT_PRIOR) {
         if (V.prior_masks[c] > 0 && V.init_costs[c] >= 0.1f) {
             const float pert = 0.02f;
             const float4 pp = V.prior_planes[c];
@@ -466,6 +477,10 @@ __device__ void init_pixel(const DevView& V, const DevParams& prm, int px, int p
         pl.w = distance_to_origin(rc, px, py, depth, pl);
     }
     Patch<NS> P;
+    if constexpr (NS > 0) {
+        P.pw = pw;
+        P.pstride = pstride;
+    }
     make_patch<S, NS>(P, S(V, 0), V, prm, px, py, q);
     const Hyp h = make_hyp(rc, pl);
     int valid = 0;
@@ -514,7 +529,7 @@ __device__ void init_pixel(const DevView& V, const DevParams& prm, int px, int p
 // NCC loop.
 template <class S, int NS>
 __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int py, int iter, int colour, float* my,
-                            int npix, const Pair& q) {
+                            int npix, const Pair& q, float2* pw, int pstride) {
     const int W = V.W, H = V.H, N = V.N, nmax = prm.nmax;
     const int center = py * W + px;
     const int same = iter & 1;
@@ -523,8 +538,8 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
     const float* __restrict__ cs = V.cost[same];
     const float* __restrict__ co = V.cost[opp];
     const DevCam& rc = V.cam[0];
-    const bool geom = prm.sweep_kind == GMVS_SWEEP_GEOM;
-    const bool prior_mode = prm.sweep_kind == GMVS_SWEEP_PRIOR;
+    const bool geom = V.sweep_kind == GMVS_SWEEP_GEOM;
+    const bool prior_mode = V.sweep_kind == GMVS_SWEEP_PRIOR;
 #define CA(k, i) my[((k) * nmax + (i)) * npix]
 #define VW(i) my[(8 * nmax + (i)) * npix]
 #define POS(k) (*reinterpret_cast<int*>(&my[(9 * nmax + (k)) * npix]))
@@ -532,8 +547,12 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
 #define PL4(slot, c) my[(9 * nmax + 16 + 4 * (slot) + (c)) * npix]
 
     DevRng rng(prm.seed_lo, prm.seed_hi, (uint32_t)center, (uint32_t)V.stream_id,
-               phase_of(prm.pass_index, 1 + 2 * iter + colour));
+               phase_of(V.pass_index, 1 + 2 * iter + colour));
     Patch<NS> P;
+    if constexpr (NS > 0) {
+        P.pw = pw;
+        P.pstride = pstride;
+    }
     make_patch<S, NS>(P, S(V, 0), V, prm, px, py, q);
 
     // Adaptive checkerboard sampling.  pos = linear index; the buffer of a

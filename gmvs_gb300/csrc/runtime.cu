@@ -278,8 +278,11 @@ Layout make_layout(const gmvs_view_pass* views, int32_t n, const gmvs_params* p,
     return L;
 }
 
-void fill_view(DevView& D, const gmvs_view_pass& V) {
+void fill_view(DevView& D, const gmvs_view_pass& V, const gmvs_params* p) {
     std::memset(&D, 0, sizeof(D));
+    D.init_kind = p->init_kind;
+    D.sweep_kind = p->sweep_kind;
+    D.pass_index = p->pass_index;
     D.H = V.height;
     D.W = V.width;
     D.N = V.num_src;
@@ -476,7 +479,7 @@ int32_t build_plan(gmvs_plan* P, const gmvs_view_pass* views, int32_t n, const g
     for (size_t s = 0; s < L.slots.size(); ++s)
         if (P->variant == kVarTex) slot_tex[(int)s] = P->texs[tex_i++];
     for (int v = 0; v < n; ++v) {
-        fill_view(hv[v], views[v]);
+        fill_view(hv[v], views[v], p);
         for (int i = 0; i <= views[v].num_src; ++i) {
             const ImageSlot& s = L.slots[L.view_slots[v][i]];
             hv[v].img[i] = s.offset == ~(size_t)0 ? (const void*)s.src : (const void*)(P->ws + s.offset);
@@ -510,8 +513,9 @@ int32_t build_plan(gmvs_plan* P, const gmvs_view_pass* views, int32_t n, const g
     if (e != cudaSuccess) return fail_cuda(e, "uploading plan descriptors");
     const int npix = TW * TH;
     const int grid = std::max(1, std::min(L.ntiles, num_sms() * 16));
-    P->init_ls = LaunchShape{grid, dim3(2 * TW, TH), (size_t)2 * nmax * npix * 4};
-    P->sweep_ls = LaunchShape{grid, dim3(2 * TW, TH), (size_t)(9 * nmax + 28) * npix * 4};
+    const size_t patch_bytes = (size_t)18 * (2 * TW * TH) * 8;  // kPatchSlots float2 per thread
+    P->init_ls = LaunchShape{grid, dim3(2 * TW, TH), (size_t)2 * nmax * npix * 4 + patch_bytes};
+    P->sweep_ls = LaunchShape{grid, dim3(2 * TW, TH), (size_t)(9 * nmax + 28) * npix * 4 + patch_bytes};
     P->fin_ls = LaunchShape{grid, dim3(TW, TH), 0};
     P->num_stages = 2 * p->max_iterations + 4;
     P->final_buf = p->max_iterations & 1;
