@@ -331,7 +331,7 @@ __device__ __forceinline__ float4 normal_to_cam(const DevCam& c, float4 p) {
 }
 
 // GenerateRandomNormal (patch_match_kernel.cu:137-172); rejection bounded at 64.
-__device__ __noinline__ float4 random_normal(const DevCam& c, int px, int py, DevRng& rng, float depth) {
+static __device__ __noinline__ float4 random_normal(const DevCam& c, int px, int py, DevRng& rng, float depth) {
     float q1 = 1.0f, q2 = 1.0f, s = 2.0f;
     for (int it = 0; it < 64 && s >= 1.0f; ++it) {
         q1 = 2.0f * rng.uniform() - 1.0f;
@@ -356,7 +356,7 @@ __device__ __noinline__ float4 random_normal(const DevCam& c, int px, int py, De
 }
 
 // GeneratePerturbedNormal (patch_match_kernel.cu:174-213)
-__device__ __noinline__ float4 perturbed_normal(const DevCam& c, int px, int py, float4 n, DevRng& rng, float pert) {
+static __device__ __noinline__ float4 perturbed_normal(const DevCam& c, int px, int py, float4 n, DevRng& rng, float pert) {
     const float4 vd = view_direction(c, px, py, 1.0f);
     const float a1 = (rng.uniform() - 0.5f) * pert;
     const float a2 = (rng.uniform() - 0.5f) * pert;
@@ -374,7 +374,7 @@ __device__ __noinline__ float4 perturbed_normal(const DevCam& c, int px, int py,
 }
 
 // compute_geom_consistency_cost (gmvs/src/patch_match.cu:562-593)
-__device__ __noinline__ float geom_cost(const DevView& V, int j, float4 pl, int px, int py) {
+static __device__ __noinline__ float geom_cost(const DevView& V, int j, float4 pl, int px, int py) {
     const DevCam& rc = V.cam[0];
     const DevCam& sc = V.cam[j + 1];
     const float depth = depth_from_plane(rc, pl, px, py);
@@ -406,7 +406,7 @@ __device__ __forceinline__ PriorK prior_k(const DevView& V) {
     k.beta = 0.18f;
     return k;
 }
-__device__ __noinline__ float restricted(const PriorK& k, float cost, float dd, float ac) {
+static __device__ __noinline__ float restricted(const PriorK& k, float cost, float dd, float ac) {
     const float ad = pmath::acosf_(ac);
     const float pr = k.gamma + pmath::expf_(-dd * dd / k.two_dsq) * pmath::expf_(-ad * ad / k.two_asq);
     return pmath::expf_(-cost * cost / k.beta) * pr;
