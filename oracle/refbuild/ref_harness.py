@@ -149,9 +149,15 @@ def camera(K, R, t, h, w, dmin, dmax) -> Camera:
     return c
 
 
-def run_patch_match(drv: Driver, cams, ref: int, src, images, depths, normals, max_iterations: int):
+def run_patch_match(drv: Driver, cams, ref: int, src, images, depths, normals, max_iterations: int,
+                    timings: dict = None):
     """PatchMatcher::run_patch_match for one problem (patch_match.cu:1353-1518);
-    images/depths [V, H, W] and normals [V, H, W, 3] are indexed by view id."""
+    images/depths [V, H, W] and normals [V, H, W, 3] are indexed by view id.
+    `timings` (optional) receives the seconds spent in uploads, kernels
+    (each followed by the reference's cudaDeviceSynchronize) and downloads."""
+    import time
+
+    t0 = time.perf_counter()
     V, H, W = images.shape
     p = default_params()
     p.max_iterations = max_iterations
@@ -172,6 +178,8 @@ def run_patch_match(drv: Driver, cams, ref: int, src, images, depths, normals, m
     d_cost = drv.alloc(4 * H * W)
     g16 = ((W + 15) // 16, (H + 15) // 16)
     gcb = ((W + 15) // 16, ((H // 2) + 15) // 16)
+    drv._ck(drv.cu.cuCtxSynchronize(), "sync")
+    t1 = time.perf_counter()
     drv.launch("initialization", g16, (16, 16), [d_img, d_dep, d_nrm, d_cam, d_plane, d_cost, d_rand, d_sel, p])
     for i in range(max_iterations):
         for black in (True, False):
@@ -183,8 +191,13 @@ def run_patch_match(drv: Driver, cams, ref: int, src, images, depths, normals, m
     od, on, oc = drv.alloc(4 * H * W), drv.alloc(12 * H * W), drv.alloc(4 * H * W)
     drv.launch("export_plane_hypotheses_cost", (((H * W) - 1) // 256 + 1,), (256,),
                [d_plane, d_cost, ctypes.c_int32(H), ctypes.c_int32(W), od, on, oc])
+    t2 = time.perf_counter()
     out = (drv.get(od, (H, W), np.float32), drv.get(on, (H, W, 3), np.float32), drv.get(oc, (H, W), np.float32))
     drv.free_all()
+    if timings is not None:
+        timings["upload_s"] = timings.get("upload_s", 0.0) + (t1 - t0)
+        timings["kernels_s"] = timings.get("kernels_s", 0.0) + (t2 - t1)
+        timings["download_s"] = timings.get("download_s", 0.0) + (time.perf_counter() - t2)
     return out
 
 
