@@ -22,6 +22,7 @@ INIT_RANDOM, INIT_PRIOR, INIT_DEPTH_NORMAL = 0, 1, 2
 SWEEP_PHOTO, SWEEP_PRIOR, SWEEP_GEOM = 0, 1, 2
 SAMPLER_CLAMP, SAMPLER_TEX = 0, 1
 STAGE_F32, STAGE_QUAD_F32, STAGE_QUAD_F16, STAGE_AUTO = 0, 1, 2, 3
+FUSE_FIXED_MAX_PIXELS = 1 << 22
 
 _f = ctypes.c_float
 _i = ctypes.c_int32
@@ -82,6 +83,7 @@ _SIGS = {
                             ctypes.c_size_t, _p]),
     "gmvs_fuse_scratch_bytes": (ctypes.c_size_t, [_i, _i]),
     "gmvs_fuse": (_i, [ctypes.POINTER(gmvs_fuse_view), _p, ctypes.c_size_t, _p]),
+    "gmvs_fuse_fixed_scratch": (_i, [ctypes.POINTER(gmvs_fuse_view), _p]),
     "gmvs_build_planar_prior": (_i, [ctypes.POINTER(gmvs_camera), _i, _i, _p, _p, _p, _i, _f, _f, _p, _p,
                                      ctypes.POINTER(_i), _p, _i]),
     "gmvs_fusion_planar_mask": (_i, [_p, _p, _p, _i, _i, _i, _f, _f, _f, _p]),

@@ -37,6 +37,7 @@ SOURCES = {
     "pm_tex.cu": [],
     "runtime.cu": [],
     "fusion.cu": [],
+    "fuse_fixed.cu": [],
     "prior.cpp": [],
 }
 

@@ -12,6 +12,7 @@
 
 #include "common.cuh"
 #include "errors.h"
+#include "kernels.h"
 
 namespace gmvs {
 namespace {
@@ -155,7 +156,7 @@ int sm_count() {
 
 }  // namespace
 
-// Shared by gmvs_fuse and the fixed-scratch variant.
+// Shared by gmvs_fuse and gmvs_fuse_fixed_scratch (fuse_fixed.cu).
 int32_t fuse_run(const gmvs_fuse_view* a, int* winner, cudaStream_t st) {
     if (!a) return fail(GMVS_ERR_INVALID, "args is NULL");
     const gmvs_problem& pb = a->problem;

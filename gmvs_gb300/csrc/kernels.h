@@ -48,4 +48,8 @@ cudaError_t launch_convert(const LaunchShape&, const DevView*, const Tile*, cons
 cudaError_t launch_filter(const LaunchShape&, const DevView*, const Tile*, const int*, int final_buf, int colour,
                           int run_filter, cudaStream_t);
 
+// Fusion of one view (fusion.cu) with a given per-pixel winner scratch of
+// height * width ints; the call re-initialises the scratch on `st`.
+int32_t fuse_run(const gmvs_fuse_view* a, int* winner, cudaStream_t st);
+
 }  // namespace gmvs

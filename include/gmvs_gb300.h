@@ -213,6 +213,25 @@ GMVS_API size_t gmvs_fuse_scratch_bytes(int32_t height, int32_t width);
 GMVS_API int32_t gmvs_fuse(const gmvs_fuse_view* args, void* scratch, size_t scratch_bytes,
                   void* stream);
 
+/* gmvs_fuse without any device allocation.  No counterpart in the reference
+ * (Fuser::run_fusion, gmvs/src/fusion.cu:211-275, allocates per call).
+ * For callers that have no device allocator at hand and may not allocate at
+ * the point of the call: a plain C / FFI caller that would otherwise need a
+ * cudaMalloc per call for gmvs_fuse's scratch, or a job running under a
+ * fixed device-memory budget, where an allocation in the middle of the job
+ * could fail.  Same inputs, outputs and results as gmvs_fuse; the per-pixel
+ * scratch is a library-owned device array of GMVS_FUSE_FIXED_MAX_PIXELS
+ * int32 entries (16 MiB), and views with height * width above that are
+ * rejected with GMVS_ERR_INVALID.  The first call on each device (the
+ * device current at the call) looks the array up, which may load a module:
+ * make that first call before any stream capture.  Every call re-initialises
+ * the part of the array it uses on `stream`, so nothing has to be cleared
+ * beforehand; but all calls on a device share the one array, so calls whose
+ * work can overlap on the device (different streams, several host threads)
+ * race and must be serialised by the caller. */
+#define GMVS_FUSE_FIXED_MAX_PIXELS (1 << 22)
+GMVS_API int32_t gmvs_fuse_fixed_scratch(const gmvs_fuse_view* args, void* stream);
+
 /* -------------------------------------------------- host (CPU) routines --
  * Planar prior from a depth/cost map: support points, Delaunay
  * triangulation, superpixel filter, rasterisation and plane fit
