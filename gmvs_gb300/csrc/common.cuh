@@ -121,6 +121,30 @@ __device__ __forceinline__ uint32_t phase_of(int pass_index, int step) {
     return ((uint32_t)pass_index << 8) | (uint32_t)step;
 }
 
+// ------------------------------------------------------------ tile queue --
+// q[0] = tiles in the list, q[1] = next unit to claim, q[2] = warps done.
+// A unit is one thread row of one tile (16 pixel columns of one row pair).
+// Warps claim units in list order, so the units in flight at any moment are
+// one compact run of the list -- a band of rows of one view -- whose source
+// footprint stays in L2; a static stride over the list lets the resident
+// CTAs drift apart across the whole batch and thrash L2 at full size.  The
+// last warp to finish resets the queue for the next launch on the stream.
+__device__ __forceinline__ int claim_unit(int* q, unsigned lane) {
+    int u = 0;
+    if (lane == 0) u = atomicAdd(q + 1, 1);
+    return __shfl_sync(0xffffffffu, u, 0);
+}
+__device__ __forceinline__ void release_queue(int* q, unsigned lane) {
+    if (lane == 0) {
+        __threadfence();
+        const int warps = (int)(gridDim.x * blockDim.y);
+        if (atomicAdd(q + 2, 1) == warps - 1) {
+            q[1] = 0;
+            q[2] = 0;
+        }
+    }
+}
+
 // --------------------------------------------------------------- helpers --
 __device__ __forceinline__ float lerpf(float a, float b, float w) { return fmaf(w, b - a, a); }
 

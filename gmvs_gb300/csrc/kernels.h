@@ -14,33 +14,34 @@ struct LaunchShape {
     int grid;      // CTAs (persistent: each loops over tiles)
     dim3 block;    // (tile width, tile thread rows)
     size_t smem;   // dynamic shared memory bytes
+    int sms = 1;   // SMs of the device (queue kernels: grid = resident CTAs)
 };
 
 // One entry per variant, defined in pm_<variant>.cu.
-cudaError_t launch_init_f32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*, int*,
+cudaError_t launch_init_f32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*, int*,
                             bool generic, cudaStream_t);
-cudaError_t launch_sweep_f32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*, int,
+cudaError_t launch_sweep_f32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*, int,
                              int*, bool generic, cudaStream_t);
-cudaError_t launch_init_qf32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*, int*,
+cudaError_t launch_init_qf32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*, int*,
                              bool generic, cudaStream_t);
-cudaError_t launch_sweep_qf32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*, int,
+cudaError_t launch_sweep_qf32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*, int,
                               int*, bool generic, cudaStream_t);
-cudaError_t launch_init_qf16(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*, int*,
+cudaError_t launch_init_qf16(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*, int*,
                              bool generic, cudaStream_t);
-cudaError_t launch_sweep_qf16(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*, int,
+cudaError_t launch_sweep_qf16(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*, int,
                               int*, bool generic, cudaStream_t);
-cudaError_t launch_init_tex(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*, int*,
+cudaError_t launch_init_tex(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*, int*,
                             bool generic, cudaStream_t);
-cudaError_t launch_sweep_tex(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*, int, int*,
+cudaError_t launch_sweep_tex(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*, int, int*,
                              bool generic, cudaStream_t);
 // Per-pixel NCC cost matrix of given hypotheses (gmvs_ncc_costs).
-cudaError_t launch_ncc_f32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*,
+cudaError_t launch_ncc_f32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*,
                            const float4*, float*, float*, uint32_t*, bool generic, cudaStream_t);
-cudaError_t launch_ncc_qf32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*,
+cudaError_t launch_ncc_qf32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*,
                             const float4*, float*, float*, uint32_t*, bool generic, cudaStream_t);
-cudaError_t launch_ncc_qf16(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*,
+cudaError_t launch_ncc_qf16(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*,
                             const float4*, float*, float*, uint32_t*, bool generic, cudaStream_t);
-cudaError_t launch_ncc_tex(const LaunchShape&, const DevView*, const DevParams&, const Tile*, const int*,
+cudaError_t launch_ncc_tex(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*,
                            const float4*, float*, float*, uint32_t*, bool generic, cudaStream_t);
 
 // Finalisation (runtime.cu): conversion, filter + export of one colour.

@@ -141,7 +141,7 @@ struct ImageSlot {
 };
 
 struct Layout {
-    size_t header = 0;     // error word + tile count
+    size_t header = 0;     // error word + tile queue
     size_t views = 0;
     size_t tiles = 0;
     size_t images = 0;
@@ -382,7 +382,7 @@ struct gmvs_plan {
     bool generic = false;
     char* ws = nullptr;
     int* d_err = nullptr;
-    int* d_ntiles = nullptr;
+    int* d_ntiles = nullptr;  // tile queue: count, next unit, warps done
     DevView* d_views = nullptr;
     Tile* d_tiles = nullptr;
     int ntiles = 0;
@@ -503,7 +503,7 @@ int32_t build_plan(gmvs_plan* P, const gmvs_view_pass* views, int32_t n, const g
         for (int y = 0; y < hh; y += TH)
             for (int x = 0; x < views[v].width; x += TW) ht.push_back(Tile{v, x, y, -1});
     }
-    int hdr[2] = {0, L.ntiles};
+    int hdr[4] = {0, L.ntiles, 0, 0};  // error word, tile queue (count, next unit, warps done)
     cudaError_t e = cudaMemcpyAsync(P->ws, hdr, sizeof(hdr), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(P->d_views, hv.data(), sizeof(DevView) * n, cudaMemcpyHostToDevice, st);
@@ -514,9 +514,10 @@ int32_t build_plan(gmvs_plan* P, const gmvs_view_pass* views, int32_t n, const g
     const int npix = TW * TH;
     const int grid = std::max(1, std::min(L.ntiles, num_sms() * 16));
     const size_t patch_bytes = (size_t)18 * (2 * TW * TH) * 8;  // kPatchSlots float2 per thread
-    P->init_ls = LaunchShape{grid, dim3(2 * TW, TH), (size_t)2 * nmax * npix * 4 + patch_bytes};
-    P->sweep_ls = LaunchShape{grid, dim3(2 * TW, TH), (size_t)(9 * nmax + 28) * npix * 4 + patch_bytes};
-    P->fin_ls = LaunchShape{grid, dim3(TW, TH), 0};
+    const int sms = num_sms();
+    P->init_ls = LaunchShape{grid, dim3(2 * TW, TH), (size_t)2 * nmax * npix * 4 + patch_bytes, sms};
+    P->sweep_ls = LaunchShape{grid, dim3(2 * TW, TH), (size_t)(9 * nmax + 28) * npix * 4 + patch_bytes, sms};
+    P->fin_ls = LaunchShape{grid, dim3(TW, TH), 0, sms};
     P->num_stages = 2 * p->max_iterations + 4;
     P->final_buf = p->max_iterations & 1;
     return GMVS_OK;
@@ -554,10 +555,14 @@ int32_t launch_stage(gmvs_plan* P, int stage, cudaStream_t st) {
     cudaError_t e = cudaSuccess;
     const DevView* dv = P->d_views;
     const Tile* dt = P->d_tiles;
-    const int* nt = P->d_ntiles;
+    int* nt = P->d_ntiles;
     if (stage == 0) {
         int32_t rc = restage(P, st);
         if (rc != GMVS_OK) return rc;
+        // the queue kernels reset it when they finish; clear it here too so a
+        // chain that was interrupted by an error starts clean
+        e = cudaMemsetAsync(nt + 1, 0, 2 * sizeof(int), st);
+        if (e != cudaSuccess) return fail_cuda(e, "resetting the tile queue");
         switch (P->variant) {
             case kVarF32: e = launch_init_f32(P->init_ls, dv, P->dprm, dt, nt, P->d_err, P->generic, st); break;
             case kVarQuadF32: e = launch_init_qf32(P->init_ls, dv, P->dprm, dt, nt, P->d_err, P->generic, st); break;

@@ -51,9 +51,10 @@ def main(nviews: int = 4) -> None:
         for ref, src in problems:
             ids = [ref] + list(src)
             dmin, dmax = sc.depth_range[0] * 0.6, sc.depth_range[1] * 1.2
-            out.append(engine.ViewInputs(cams=[gcams[i] for i in ids], images=[gi[i] for i in ids], depth_min=dmin,
-                                         depth_max=dmax, stream_id=ref, depths=[gd[i] for i in ids],
-                                         ref_normal=gn[ref]))
+            v = engine.ViewInputs(cams=[gcams[i] for i in ids], images=[gi[i] for i in ids], depth_min=dmin,
+                                  depth_max=dmax, stream_id=ref, depths=[gd[i] for i in ids], ref_normal=gn[ref])
+            v.allocate_outputs()
+            out.append(v)
         return out
 
     p = engine.params_struct(init_kind=_abi.INIT_DEPTH_NORMAL, sweep_kind=_abi.SWEEP_GEOM,
