@@ -1,0 +1,116 @@
+"""Launch-shape autotuner for the PatchMatch kernels.
+
+The knobs that change speed but not results are the tile height (a tile is
+16 pixel columns by 2 * tile_h rows; tile_h thread rows of one warp each per
+CTA, so tile_h = 8 is a 16 x 16 tile and 4 a 16 x 8 tile) and the resident
+CTAs per SM (fewer CTAs leave more of the 256 KB of L1/shared memory to the
+sample cache, more CTAs hide more latency).  The window stride
+(radius_increment) is a parameter of the method -- stride 1 and 2 give
+different costs -- so it is not tuned: each stride is tuned on its own and
+keyed separately.
+
+A tuning run times whole plan launches (init, every half-sweep, filter) of a
+representative subset of the batch's views with CUDA events and keeps the
+fastest candidate.  Results are cached per key (sampler, staging, sweep
+kind, largest source count, window, image-size class) in memory and,
+optionally, in a JSON file.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import json
+import math
+import os
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import torch
+
+from . import _abi
+from .engine import Plan, ViewInputs, Workspace
+
+TILE_HEIGHTS = (2, 4, 8)
+CTAS_PER_SM = (0, 3, 2)
+CANDIDATES: Tuple[Tuple[int, int], ...] = tuple((th, c) for th in TILE_HEIGHTS for c in CTAS_PER_SM)
+
+
+def _copy_params(p: _abi.gmvs_params) -> _abi.gmvs_params:
+    q = _abi.gmvs_params()
+    ctypes.memmove(ctypes.byref(q), ctypes.byref(p), ctypes.sizeof(p))
+    return q
+
+
+def tune_key(views: Sequence[ViewInputs], params: _abi.gmvs_params) -> str:
+    nmax = max(len(v.images) - 1 for v in views)
+    px = max(v.height * v.width for v in views)
+    size_class = int(round(math.log2(max(px, 1))))
+    return (f"s{params.sampler}-st{params.staging}-sw{params.sweep_kind}-i{params.init_kind}-n{nmax}"
+            f"-p{params.patch_size}-r{params.radius_increment}-px{size_class}")
+
+
+@dataclass
+class TuneResult:
+    key: str
+    best: Tuple[int, int]
+    ms: Dict[str, float] = field(default_factory=dict)  # "tile_h,ctas" -> ms per plan launch
+
+    def apply(self, params: _abi.gmvs_params) -> _abi.gmvs_params:
+        q = _copy_params(params)
+        q.tile_h, q.ctas_per_sm = self.best
+        return q
+
+
+class Autotuner:
+    def __init__(self, cache_path: Optional[str] = None, candidates: Sequence[Tuple[int, int]] = CANDIDATES,
+                 reps: int = 2, max_views: int = 2):
+        self.cache_path = cache_path
+        self.candidates = tuple(candidates)
+        self.reps = reps
+        self.max_views = max_views
+        self.cache: Dict[str, TuneResult] = {}
+        if cache_path and os.path.exists(cache_path):
+            with open(cache_path) as f:
+                for k, v in json.load(f).items():
+                    self.cache[k] = TuneResult(k, tuple(v["best"]), v.get("ms", {}))
+
+    def _save(self) -> None:
+        if not self.cache_path:
+            return
+        data = {k: {"best": list(r.best), "ms": r.ms} for k, r in self.cache.items()}
+        tmp = self.cache_path + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+        os.replace(tmp, self.cache_path)
+
+    def tune(self, views: Sequence[ViewInputs], params: _abi.gmvs_params,
+             stream: Optional[torch.cuda.Stream] = None) -> TuneResult:
+        """Best (tile_h, ctas_per_sm) for this kind of batch (cached)."""
+        key = tune_key(views, params)
+        if key in self.cache:
+            return self.cache[key]
+        sample = list(views)[: self.max_views]
+        dev = sample[0].images[0].device
+        st = stream or torch.cuda.current_stream(dev)
+        ws = Workspace(dev)
+        ms: Dict[str, float] = {}
+        for th, c in self.candidates:
+            p = _copy_params(params)
+            p.tile_h, p.ctas_per_sm = th, c
+            plan = Plan(sample, p, ws, st)
+            try:
+                plan.launch(st)  # warm-up (module load, first-touch)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                for _ in range(self.reps):
+                    plan.launch(st)
+                e1.record(st)
+                plan.check(st)
+                ms[f"{th},{c}"] = e0.elapsed_time(e1) / self.reps
+            finally:
+                plan.close()
+        best = min(ms, key=ms.get)
+        res = TuneResult(key, tuple(int(x) for x in best.split(",")), ms)
+        self.cache[key] = res
+        self._save()
+        return res

@@ -15,6 +15,7 @@ struct LaunchShape {
     dim3 block;    // (tile width, tile thread rows)
     size_t smem;   // dynamic shared memory bytes
     int sms = 1;   // SMs of the device (queue kernels: grid = resident CTAs)
+    int ctas = 0;  // resident CTAs per SM wanted (0 = as many as fit)
 };
 
 // One entry per variant, defined in pm_<variant>.cu.

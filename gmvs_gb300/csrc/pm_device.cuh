@@ -92,13 +92,18 @@ struct SampTex {
 // round-to-nearest reciprocal for every significand at 30 binary exponents
 // between 2^-125 and 2^125 of both signs: identical.  Outside that range
 // (and for 0, inf, NaN) the IEEE reciprocal is used.
-__device__ __forceinline__ float rcp_rn(float x) {
-    const float ax = fabsf(x);
-    if (!(ax >= 2.35098870e-38f && ax <= 4.25352959e+37f)) return __frcp_rn(x);  // 2^-125, 2^125
+constexpr float kRcpLo = 2.35098870e-38f, kRcpHi = 4.25352959e+37f;  // 2^-125, 2^125
+// the refined approximation alone: callers guarantee kRcpLo <= |x| <= kRcpHi
+__device__ __forceinline__ float rcp_in_range(float x) {
     float y;
     asm("rcp.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
     const float e = __fmaf_rn(-x, y, 1.0f);
     return __fmaf_rn(y, e, y);
+}
+__device__ __forceinline__ float rcp_rn(float x) {
+    const float ax = fabsf(x);
+    if (!(ax >= kRcpLo && ax <= kRcpHi)) return __frcp_rn(x);
+    return rcp_in_range(x);
 }
 
 // -------------------------------------------------------- reference patch --
@@ -236,24 +241,52 @@ __device__ __forceinline__ float ncc_cost(const DevView& V, const DevParams& prm
         float qys[NS];
 #pragma unroll
         for (int bb = 0; bb < NS; ++bb) qys[bb] = (float)window_coord<S>(py, -radius + bb * inc, V.H);
-#pragma unroll 1
-        for (int al = 0; al < NC; ++al) {
-            const float qx = (float)window_coord<S>(px, -radius + (q.h * NC + al) * inc, V.W);
-            const float bx = fmaf(m0, qx, m2), by = fmaf(m3, qx, m5), bz = fmaf(m6, qx, m8);
+        const float qx0 = (float)window_coord<S>(px, -radius + (q.h * NC) * inc, V.W);
+        const float qx1 = (float)window_coord<S>(px, -radius + (q.h * NC + NC - 1) * inc, V.W);
+        // The projective depth z = fma(m7, qy, fma(m6, qx, m8)) is monotone in
+        // qx and in qy (a rounded fma is monotone in its addend, and in its
+        // multiplicand for a fixed multiplier), so over this lane's part of
+        // the window it is extreme at the four corners.  When the corners lie
+        // on one side of zero inside the range where the refined reciprocal
+        // is exact, every sample does, and the per-sample range test drops.
+        const float bz0 = fmaf(m6, qx0, m8), bz1 = fmaf(m6, qx1, m8);
+        const float za = fmaf(m7, qys[0], bz0), zb = fmaf(m7, qys[NS - 1], bz0);
+        const float zc = fmaf(m7, qys[0], bz1), zd = fmaf(m7, qys[NS - 1], bz1);
+        const float zlo = fminf(fminf(za, zb), fminf(zc, zd)), zhi = fmaxf(fmaxf(za, zb), fmaxf(zc, zd));
+        const bool in_range = (zlo >= kRcpLo && zhi <= kRcpHi) || (zhi <= -kRcpLo && zlo >= -kRcpHi);
+#define GMVS_SAMPLE_COLUMN(RCP, ROWS)                                                              \
+    {                                                                                              \
+        const float qx = (float)window_coord<S>(px, -radius + (q.h * NC + al) * inc, V.W);        \
+        const float bx = fmaf(m0, qx, m2), by = fmaf(m3, qx, m5), bz = fmaf(m6, qx, m8);           \
+        _Pragma(ROWS) for (int bb = 0; bb < NS; ++bb) {                                            \
+            const float qy = qys[bb];                                                              \
+            const float rz = RCP(fmaf(m7, qy, bz));                                                \
+            const float u = fmaf(m1, qy, bx) * rz;                                                 \
+            const float v = fmaf(m4, qy, by) * rz;                                                 \
+            const float s = src.sample(u, v);                                                      \
+            const float2 wt = P.pw[(al * NS + bb) * P.pstride];                                    \
+            const float ws = wt.x * s;                                                             \
+            ss += ws;                                                                              \
+            sss = fmaf(ws, s, sss);                                                                \
+            srs = fmaf(wt.y, s, srs);                                                              \
+        }                                                                                          \
+    }
+        if (in_range) {
+            if constexpr (S::kTex) {
+                // one instruction per sample: unroll the columns too, so all
+                // of this lane's fetches can be in flight together
 #pragma unroll
-            for (int bb = 0; bb < NS; ++bb) {
-                const float qy = qys[bb];
-                const float rz = rcp_rn(fmaf(m7, qy, bz));
-                const float u = fmaf(m1, qy, bx) * rz;
-                const float v = fmaf(m4, qy, by) * rz;
-                const float s = src.sample(u, v);
-                const float2 wt = P.pw[(al * NS + bb) * P.pstride];
-                const float ws = wt.x * s;
-                ss += ws;
-                sss = fmaf(ws, s, sss);
-                srs = fmaf(wt.y, s, srs);
+                for (int al = 0; al < NC; ++al) GMVS_SAMPLE_COLUMN(rcp_in_range, "unroll")
+            } else {
+                // software-interpolated samples: keep the code compact
+#pragma unroll 1
+                for (int al = 0; al < NC; ++al) GMVS_SAMPLE_COLUMN(rcp_in_range, "unroll")
             }
+        } else {
+#pragma unroll 1
+            for (int al = 0; al < NC; ++al) GMVS_SAMPLE_COLUMN(rcp_rn, "unroll 1")
         }
+#undef GMVS_SAMPLE_COLUMN
     } else {
         const int radius = prm.patch_size / 2;
         const int inc = prm.radius_increment;

@@ -193,6 +193,8 @@ int32_t validate(const gmvs_view_pass* views, int32_t n, const gmvs_params* p) {
     if (p->init_kind < 0 || p->init_kind > 2 || p->sweep_kind < 0 || p->sweep_kind > 2)
         return fail(GMVS_ERR_INVALID, "unknown init_kind / sweep_kind");
     if (p->tile_h < 0 || p->tile_h > 8) return fail(GMVS_ERR_INVALID, "tile_h must be in [0, 8]");
+    if (p->tile_w != 0 && p->tile_w != 16) return fail(GMVS_ERR_INVALID, "tile_w must be 0 or 16");
+    if (p->ctas_per_sm < 0 || p->ctas_per_sm > 32) return fail(GMVS_ERR_INVALID, "ctas_per_sm must be in [0, 32]");
     for (int v = 0; v < n; ++v) {
         const gmvs_view_pass& V = views[v];
         if (V.height < 1 || V.width < 1) return fail(GMVS_ERR_INVALID, "view " + std::to_string(v) + ": empty image");
@@ -515,9 +517,10 @@ int32_t build_plan(gmvs_plan* P, const gmvs_view_pass* views, int32_t n, const g
     const int grid = std::max(1, std::min(L.ntiles, num_sms() * 16));
     const size_t patch_bytes = (size_t)18 * (2 * TW * TH) * 8;  // kPatchSlots float2 per thread
     const int sms = num_sms();
-    P->init_ls = LaunchShape{grid, dim3(2 * TW, TH), (size_t)2 * nmax * npix * 4 + patch_bytes, sms};
-    P->sweep_ls = LaunchShape{grid, dim3(2 * TW, TH), (size_t)(9 * nmax + 28) * npix * 4 + patch_bytes, sms};
-    P->fin_ls = LaunchShape{grid, dim3(TW, TH), 0, sms};
+    const int ctas = p->ctas_per_sm;
+    P->init_ls = LaunchShape{grid, dim3(2 * TW, TH), (size_t)2 * nmax * npix * 4 + patch_bytes, sms, ctas};
+    P->sweep_ls = LaunchShape{grid, dim3(2 * TW, TH), (size_t)(9 * nmax + 28) * npix * 4 + patch_bytes, sms, ctas};
+    P->fin_ls = LaunchShape{grid, dim3(TW, TH), 0, sms, 0};
     P->num_stages = 2 * p->max_iterations + 4;
     P->final_buf = p->max_iterations & 1;
     return GMVS_OK;

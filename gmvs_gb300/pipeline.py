@@ -54,9 +54,18 @@ class ScenePipeline:
     """Runs the five stages for one scene; buffers are kept for reuse."""
 
     def __init__(self, scene: SceneInputs, geom_iters: int = 2, geom_consistent: int = 3, mode: str = "batched",
-                 staging: int = _abi.STAGE_AUTO, tile_h: int = 0, prior_threads: int = 8, params=None):
+                 staging: int = _abi.STAGE_AUTO, tile_h: int = 0, prior_threads: int = 8, params=None,
+                 graphs: bool = False, autotuner=None):
         if mode not in ("batched", "plain"):
             raise ValueError("mode is 'batched' or 'plain'")
+        if graphs and mode != "batched":
+            raise ValueError("CUDA graphs replay the batched launch chains")
+        self.graphs = graphs
+        self._graphs: Dict[str, torch.cuda.CUDAGraph] = {}
+        if autotuner is not None and mode != "batched":
+            raise ValueError("the autotuner picks launch shapes of the batched launch chains")
+        self.autotuner = autotuner
+        self.tuned: Dict[str, object] = {}
         self.sc = scene
         self.geom_iters = geom_iters
         self.gc = geom_consistent
@@ -121,32 +130,88 @@ class ScenePipeline:
             p.max_iterations = self.base.geom_max_iterations
         return p
 
+    def _passes(self):
+        """(key, kind, output buffer, input buffer, pass index) of every pass."""
+        out = [("random", "random", 0, None, 0), ("prior", "prior", 1, 0, 1)]
+        buf = 1
+        for g in range(self.geom_iters):
+            out.append((f"geom{g}", "geom", 1 - buf, buf, 2 + g))
+            buf = 1 - buf
+        return out
+
+    def prepare(self, stream: Optional[torch.cuda.Stream] = None) -> None:
+        """Create every pass's plan now (batched mode; plan creation
+        synchronises `stream`) and, with ``graphs``, capture each pass's
+        launch chain into a CUDA graph.  Needs the images in place.  With an
+        autotuner, a pass whose launch shape is not tuned yet is prepared at
+        its first launch instead, when its inputs exist to tune on."""
+        if self.mode != "batched":
+            return
+        for key, kind, out, src_buf, pass_index in self._passes():
+            if self.autotuner is not None:
+                from .autotune import tune_key
+
+                if tune_key(self._views(kind, out, src_buf), self._params(kind, pass_index)) \
+                        not in self.autotuner.cache:
+                    continue
+            self._ensure(key, kind, out, src_buf, pass_index, stream)
+
+    def _ensure(self, key: str, kind: str, out: int, src_buf: Optional[int], pass_index: int,
+                stream: Optional[torch.cuda.Stream]) -> None:
+        if key not in self.plans:
+            views = self._views(kind, out, src_buf)
+            p = self._params(kind, pass_index)
+            if self.autotuner is not None:
+                res = self.autotuner.tune(views, p, stream)
+                self.tuned[key] = res
+                p = res.apply(p)
+            ws = self.ws.setdefault(key, Workspace(self.sc.images.device))
+            self.plans[key] = [Plan(views, p, ws, stream)]
+        if self.graphs and key not in self._graphs:
+            g = torch.cuda.CUDAGraph()
+            side = torch.cuda.Stream(device=self.sc.images.device)
+            side.wait_stream(torch.cuda.current_stream() if stream is None else stream)
+            with torch.cuda.graph(g, stream=side, capture_error_mode="thread_local"):
+                for pl in self.plans[key]:
+                    pl.launch(side)
+            self._graphs[key] = g
+
     def _run(self, key: str, kind: str, out: int, src_buf: Optional[int], pass_index: int,
              stream: Optional[torch.cuda.Stream]) -> None:
-        p = self._params(kind, pass_index)
-        views = self._views(kind, out, src_buf)
-        ws = self.ws.setdefault(key, Workspace())
         if self.mode == "batched":
-            if key not in self.plans:
-                self.plans[key] = [Plan(views, p, ws, stream)]
-            for pl in self.plans[key]:
-                pl.launch(stream)
-        else:
-            if key not in self.plans:
-                # one workspace region per view keeps plans valid together
-                self.plans[key] = []
-            for k, v in enumerate(views):
-                plan = Plan([v], p, ws, stream)
-                for s in range(plan.num_stages):
-                    plan.launch_stage(s, stream)
-                    torch.cuda.synchronize()
-                plan.close()
+            self._ensure(key, kind, out, src_buf, pass_index, stream)
+            if self.graphs:
+                with torch.cuda.stream(stream or torch.cuda.current_stream()):
+                    self._graphs[key].replay()
+            else:
+                for pl in self.plans[key]:
+                    pl.launch(stream)
+            return
+        # plain: one plan per view, a synchronisation after every kernel
+        p = self._params(kind, pass_index)
+        ws = self.ws.setdefault(key, Workspace())
+        for v in self._views(kind, out, src_buf):
+            plan = Plan([v], p, ws, stream)
+            for s in range(plan.num_stages):
+                plan.launch_stage(s, stream)
+                torch.cuda.synchronize()
+            plan.close()
 
     def _prior(self, buf: int) -> None:
         """Host triangulation of every view (parallel over views)."""
+        planes, masks = self.triangulate(self.depth[buf].cpu().numpy(), self.cost[buf].cpu().numpy())
+        self.upload_prior(planes, masks)
+
+    def upload_prior(self, planes: np.ndarray, masks: np.ndarray,
+                     stream: Optional[torch.cuda.Stream] = None) -> None:
+        with torch.cuda.stream(stream or torch.cuda.current_stream()):
+            self.prior_planes.copy_(torch.from_numpy(planes), non_blocking=stream is not None)
+            self.prior_masks.copy_(torch.from_numpy(masks.view(np.int32)), non_blocking=stream is not None)
+
+    def triangulate(self, depth: np.ndarray, cost: np.ndarray):
+        """Planar priors of every reference view from host depth/cost maps
+        [V, H, W]; returns (planes float32 [V, H, W, 4], masks uint32 [V, H, W])."""
         sc = self.sc
-        depth = self.depth[buf].cpu().numpy()
-        cost = self.cost[buf].cpu().numpy()
         planes = np.empty((self.V, self.H, self.W, 4), np.float32)
         masks = np.empty((self.V, self.H, self.W), np.uint32)
         spf = sc.superpixels is not None
@@ -160,8 +225,7 @@ class ScenePipeline:
         refs = [r for r, _ in sc.problems]
         with ThreadPoolExecutor(self.prior_threads) as ex:
             list(ex.map(one, refs))
-        self.prior_planes.copy_(torch.from_numpy(planes))
-        self.prior_masks.copy_(torch.from_numpy(masks.view(np.int32)))
+        return planes, masks
 
     def _fuse(self, buf: int, stream: Optional[torch.cuda.Stream]) -> None:
         sc = self.sc
@@ -184,23 +248,40 @@ class ScenePipeline:
             return time.perf_counter()
 
         t = time.perf_counter()
-        self._run("random", "random", 0, None, 0, stream)
+        self.random_pass(stream)
         t = mark("random_pass", t)
         self._prior(0)
         t = mark("triangulation", t)
-        self._run("prior", "prior", 1, 0, 1, stream)
+        self.prior_pass(stream)
         t = mark("prior_pass", t)
-        buf = 1
-        for g in range(self.geom_iters):
-            self._run(f"geom{g}", "geom", 1 - buf, buf, 2 + g, stream)
-            buf = 1 - buf
+        buf = self.geom_passes(stream)
         t = mark("geom_passes", t)
-        if self.geom_iters > 0:
-            self._fuse(buf, stream)
+        self.fusion(buf, stream)
         mark("fusion", t)
         return self.fused_depth, self.fused_normal
 
+    # the stages one at a time (for schedulers that interleave scenes)
+    def random_pass(self, stream: Optional[torch.cuda.Stream] = None) -> None:
+        self._run(*self._passes()[0], stream)
+
+    def prior_pass(self, stream: Optional[torch.cuda.Stream] = None) -> None:
+        self._run(*self._passes()[1], stream)
+
+    def geom_passes(self, stream: Optional[torch.cuda.Stream] = None) -> int:
+        """Enqueue the geometric passes; returns the buffer holding the result."""
+        buf = 1
+        for args in self._passes()[2:]:
+            self._run(*args, stream)
+            buf = args[2]
+        return buf
+
+    def fusion(self, buf: int, stream: Optional[torch.cuda.Stream] = None) -> None:
+        if self.geom_iters > 0:
+            with torch.cuda.stream(stream or torch.cuda.current_stream()):
+                self._fuse(buf, stream)
+
     def close(self) -> None:
+        self._graphs.clear()
         for plans in self.plans.values():
             for p in plans:
                 p.close()

@@ -1,0 +1,282 @@
+"""Continuous-batching reconstruction server (one GPU, one process).
+
+Jobs are whole scenes (the inputs of ``launch.py``: images, cameras,
+problems, superpixels).  The server admits queued jobs in arrival order as
+soon as their device footprint fits in the memory budget and an active slot
+is free, keeps every admitted job's images, plane fields, costs and maps
+resident on the device, and advances all active jobs together: each job runs
+its passes on its own CUDA stream, so the kernels of different jobs overlap
+on the device (the tile-queue kernels of one job fill the SMs the previous
+kernel of another job leaves idle at its tail), while the host triangulation
+of one job overlaps the device work of the others.  A job that finishes
+returns its memory and the next queued job is admitted at once.
+
+Per-view latency is the time from a job's arrival to the moment its fused
+maps are on the host, counted once for each of its reference views.  Results
+do not depend on the mix: every job's kernels read only that job's buffers
+and draw random numbers from counters keyed by (pixel, reference view,
+pass), so a job returns the same maps alone and next to others.
+"""
+
+from __future__ import annotations
+
+import heapq
+import threading
+import time
+from concurrent.futures import Future, ThreadPoolExecutor
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional
+
+import numpy as np
+import torch
+
+from .pipeline import SceneInputs, ScenePipeline
+
+# Bytes per pixel of one view that ScenePipeline keeps on the device
+# (batched mode, worst-case staging):
+#   images fp32 4; depth/normal/cost/planes double-buffered 72; prior planes
+#   and masks 20; fused depth/normal 16; masks 1; texture staging of the
+#   random and prior passes 4 + 4; quad staging of each geometric pass 16.
+_PER_VIEW_BYTES = 4 + 72 + 20 + 16 + 1 + 8
+_PER_GEOM_PASS_VIEW_BYTES = 16
+# per reference view and pass: plane/cost/view-mask ping-pong + converted planes
+_PER_REF_PASS_BYTES = 64
+_FIXED_BYTES = 64 << 20  # descriptors, tile lists, fusion scratch, allocator slack
+
+
+def footprint_bytes(num_views: int, height: int, width: int, num_refs: int, geom_iters: int = 2) -> int:
+    """Upper bound of the device memory one job holds while it is active."""
+    px = height * width
+    per_view = _PER_VIEW_BYTES + geom_iters * _PER_GEOM_PASS_VIEW_BYTES
+    passes = 2 + geom_iters
+    pitch_slack = 2 * num_views * height * 256  # texture rows padded to 256 bytes
+    return px * (num_views * per_view + num_refs * passes * _PER_REF_PASS_BYTES + 4) + pitch_slack + _FIXED_BYTES
+
+
+@dataclass
+class Job:
+    """A reconstruction request.  ``images`` are host uint8 or float32
+    [V, H, W]; the result (fused depth [V, H, W], normal [V, H, W, 3]) lands
+    in ``result`` as host arrays."""
+
+    job_id: int
+    images: np.ndarray
+    cams: list
+    problems: list
+    superpixels: Optional[np.ndarray] = None
+    arrival: float = 0.0          # seconds on the server clock
+    admitted: float = -1.0
+    finished: float = -1.0
+    result: Optional[tuple] = None
+    error: Optional[BaseException] = None
+
+    @property
+    def num_views(self) -> int:
+        return int(self.images.shape[0])
+
+    @property
+    def num_refs(self) -> int:
+        return len(self.problems)
+
+    def footprint(self, geom_iters: int) -> int:
+        V, H, W = self.images.shape
+        return footprint_bytes(V, H, W, len(self.problems), geom_iters)
+
+
+@dataclass
+class _Active:
+    job: Job
+    pipe: ScenePipeline
+    stream: torch.cuda.Stream
+    bytes: int
+    step: int = 0
+    event: Optional[torch.cuda.Event] = None
+    host: Optional[Future] = None
+    pinned: Dict[str, torch.Tensor] = field(default_factory=dict)
+
+
+class ReconstructionServer:
+    """See the module docstring.  ``memory_budget`` bounds the summed
+    footprints of the active jobs (default: 90 % of the free device memory
+    when the server starts); ``max_active`` bounds the number of jobs in
+    flight."""
+
+    def __init__(self, device: Optional[torch.device] = None, memory_budget: Optional[int] = None,
+                 max_active: int = 4, geom_iters: int = 2, prior_threads: int = 8, graphs: bool = False):
+        self.device = device or torch.device("cuda", torch.cuda.current_device())
+        if memory_budget is None:
+            free, _ = torch.cuda.mem_get_info(self.device)
+            memory_budget = int(free * 0.9)
+        self.budget = int(memory_budget)
+        self.max_active = max_active
+        self.geom_iters = geom_iters
+        self.graphs = graphs
+        self.queue: List[tuple] = []       # (arrival, job_id, job)
+        self.active: List[_Active] = []
+        self.done: List[Job] = []
+        self.in_use = 0
+        self.pool = ThreadPoolExecutor(max(1, prior_threads))
+        self.prior_threads = prior_threads
+        self.t0 = time.perf_counter()
+        self._lock = threading.Lock()
+
+    # ------------------------------------------------------------- clock --
+    def now(self) -> float:
+        return time.perf_counter() - self.t0
+
+    # ----------------------------------------------------------- requests --
+    def submit(self, job: Job) -> Job:
+        """Queue a job; it is admitted once it has arrived and fits."""
+        if job.footprint(self.geom_iters) > self.budget:
+            raise ValueError(f"job {job.job_id} needs {job.footprint(self.geom_iters)} bytes, more than the "
+                             f"server's whole budget of {self.budget}")
+        with self._lock:
+            heapq.heappush(self.queue, (job.arrival, job.job_id, job))
+        return job
+
+    def _admit(self) -> None:
+        now = self.now()
+        while self.queue and len(self.active) < self.max_active:
+            arrival, _, job = self.queue[0]
+            if arrival > now:
+                return
+            need = job.footprint(self.geom_iters)
+            if self.in_use + need > self.budget:
+                return  # admission in arrival order: wait for memory
+            heapq.heappop(self.queue)
+            self._start(job, need)
+
+    def _start(self, job: Job, need: int) -> None:
+        st = torch.cuda.Stream(device=self.device)
+        with torch.cuda.stream(st):
+            host = torch.from_numpy(np.ascontiguousarray(job.images))
+            imgs = host.pin_memory().to(self.device, non_blocking=True).to(torch.float32)
+            scene = SceneInputs(images=imgs, cams=list(job.cams), problems=[(r, list(s)) for r, s in job.problems],
+                                superpixels=job.superpixels)
+            pipe = ScenePipeline(scene, geom_iters=self.geom_iters, mode="batched",
+                                 prior_threads=self.prior_threads, graphs=self.graphs)
+        st.synchronize()
+        pipe.prepare(st)
+        job.admitted = self.now()
+        self.in_use += need
+        self.active.append(_Active(job=job, pipe=pipe, stream=st, bytes=need))
+
+    # ------------------------------------------------------------ stepping --
+    def _record(self, a: _Active) -> None:
+        a.event = torch.cuda.Event()
+        a.event.record(a.stream)
+
+    def _advance(self, a: _Active) -> bool:
+        """Move one job forward if its pending work is done; True when finished."""
+        if a.event is not None and not a.event.query():
+            return False
+        if a.host is not None and not a.host.done():
+            return False
+        p, st = a.pipe, a.stream
+        if a.step == 0:  # random pass, then the depth/cost maps to the host
+            p.random_pass(st)
+            with torch.cuda.stream(st):
+                a.pinned["depth"] = torch.empty(p.depth[0].shape, dtype=torch.float32, pin_memory=True)
+                a.pinned["cost"] = torch.empty(p.cost[0].shape, dtype=torch.float32, pin_memory=True)
+                a.pinned["depth"].copy_(p.depth[0], non_blocking=True)
+                a.pinned["cost"].copy_(p.cost[0], non_blocking=True)
+            self._record(a)
+        elif a.step == 1:  # host triangulation
+            a.event = None
+            a.host = self.pool.submit(p.triangulate, a.pinned["depth"].numpy(), a.pinned["cost"].numpy())
+        elif a.step == 2:  # prior pass, geometric passes, fusion, results to the host
+            planes, masks = a.host.result()
+            a.host = None
+            p.upload_prior(planes, masks, st)
+            p.prior_pass(st)
+            buf = p.geom_passes(st)
+            p.fusion(buf, st)
+            with torch.cuda.stream(st):
+                a.pinned["fd"] = torch.empty(p.fused_depth.shape, dtype=torch.float32, pin_memory=True)
+                a.pinned["fn"] = torch.empty(p.fused_normal.shape, dtype=torch.float32, pin_memory=True)
+                a.pinned["fd"].copy_(p.fused_depth, non_blocking=True)
+                a.pinned["fn"].copy_(p.fused_normal, non_blocking=True)
+                a.pinned["planes"] = torch.from_numpy(planes)  # kept alive until the copy is done
+            self._record(a)
+        else:
+            a.job.result = (a.pinned["fd"].numpy().copy(), a.pinned["fn"].numpy().copy())
+            a.job.finished = self.now()
+            return True
+        a.step += 1
+        return False
+
+    def _retire(self, a: _Active) -> None:
+        a.pipe.close()
+        self.in_use -= a.bytes
+        self.active.remove(a)
+        self.done.append(a.job)
+
+    def poll(self) -> int:
+        """Admit what fits and advance every active job once; returns the
+        number of jobs still queued or active."""
+        self._admit()
+        for a in list(self.active):
+            try:
+                finished = self._advance(a)
+            except BaseException as e:  # a failing job does not take the others down
+                a.job.error = e
+                a.job.finished = self.now()
+                finished = True
+            if finished:
+                self._retire(a)
+                self._admit()
+        return len(self.queue) + len(self.active)
+
+    def run(self, idle_sleep: float = 0.0005) -> List[Job]:
+        """Serve until the queue is empty and every job has finished."""
+        while self.poll():
+            time.sleep(idle_sleep)
+        return self.done
+
+    def close(self) -> None:
+        for a in list(self.active):
+            a.pipe.close()
+        self.active.clear()
+        self.pool.shutdown(wait=True)
+
+
+def latency_stats(jobs: List[Job]) -> dict:
+    """p50/p99 per-view latency (ms) and sustained ref-views/s of served jobs."""
+    per_view = []
+    for j in jobs:
+        if j.error is None and j.finished >= 0:
+            per_view += [(j.finished - j.arrival) * 1000.0] * j.num_refs
+    if not per_view:
+        return {"views": 0}
+    span = max(j.finished for j in jobs) - min(j.arrival for j in jobs)
+    return {"views": len(per_view), "p50_ms": float(np.percentile(per_view, 50)),
+            "p99_ms": float(np.percentile(per_view, 99)), "ref_views_per_s": len(per_view) / span if span > 0 else None}
+
+
+def synthetic_job(job_id: int, seed: int, num_views: int, height: int, width: int, num_src: int,
+                  arrival: float = 0.0, device=None) -> Job:
+    """A room-scene job (seeded, rendered on `device`) with host images."""
+    from . import synthetic
+    from .engine import make_camera
+
+    sc = synthetic.room_scene(seed, H=height, W=width, num_views=num_views, num_src=num_src, device=device)
+    cams = [make_camera(*synthetic.camera_args(sc, i)) for i in range(sc.num_views)]
+    problems = [(r, list(s)) for r, s in sc.problems if len(s) > 0]
+    return Job(job_id=job_id, images=sc.images, cams=cams, problems=problems, superpixels=sc.superpixels,
+               arrival=arrival)
+
+
+def poisson_stream(num_jobs: int, rate: float, seed: int, sizes=((480, 640), (960, 1280), (1200, 1600)),
+                   views=(8, 16), src=(4, 10), device=None) -> List[Job]:
+    """Jobs with Poisson arrivals at `rate` jobs/s, uneven sizes and view
+    counts drawn from numpy.random.default_rng(seed)."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    jobs = []
+    for i in range(num_jobs):
+        t += float(rng.exponential(1.0 / rate))
+        H, W = sizes[int(rng.integers(len(sizes)))]
+        V = int(rng.integers(views[0], views[1] + 1))
+        N = int(min(rng.integers(src[0], src[1] + 1), V - 1))
+        jobs.append(synthetic_job(i, int(rng.integers(1 << 30)), V, H, W, N, arrival=t, device=device))
+    return jobs

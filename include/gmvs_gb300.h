@@ -112,9 +112,11 @@ typedef struct gmvs_params {
     int32_t sampler;          /* gmvs_sampler */
     int32_t staging;          /* gmvs_staging */
     int32_t pass_index;       /* decorrelates the Philox streams of successive passes */
-    int32_t tile_w;           /* sweep tile width in pixels (0 = 32) */
-    int32_t tile_h;           /* sweep tile height in thread rows (0 = 4) */
+    int32_t tile_w;           /* sweep tile width in pixels: 0 or 16 (one lane pair per pixel) */
+    int32_t tile_h;           /* sweep tile height in thread rows, 1..8 (0 = 4); a tile is 16 x 2*tile_h pixels */
     int32_t run_filter;       /* 1 = depth/normal conversion + checkerboard median filter */
+    int32_t ctas_per_sm;      /* PatchMatch kernels: resident CTAs per SM (0 = as many as fit); fewer CTAs
+                                 leave more of the SM's L1 to the texture/sample cache */
 } gmvs_params;
 
 /* One reference view of one pass.  All pointers are device pointers except

@@ -36,3 +36,15 @@ def random_planes(sc: synthetic.Scene, view: int, rng: np.random.Generator, dmin
     n[flip] = -n[flip]
     w = -np.sum(n * X, -1)
     return np.concatenate([n, w[..., None]], -1).astype(np.float32)
+
+
+def gpu_view(sc: synthetic.Scene, ids, dev, dmin, dmax, **kw):
+    """engine.ViewInputs of reference ids[0] with sources ids[1:] on `dev`."""
+    import torch
+
+    from gmvs_gb300 import engine
+
+    imgs = torch.from_numpy(sc.images[ids].astype(np.float32)).to(dev)
+    cams = [engine.make_camera(*synthetic.camera_args(sc, i)) for i in ids]
+    return engine.ViewInputs(cams=cams, images=[imgs[k] for k in range(len(ids))], depth_min=dmin, depth_max=dmax,
+                             stream_id=ids[0], **kw)

@@ -9,7 +9,7 @@ import pytest
 import torch
 
 from gmvs_gb300 import _abi, engine, synthetic
-from scenes import cam_args, gt_planes, random_planes
+from scenes import cam_args, gpu_view, gt_planes, random_planes
 
 pytestmark = pytest.mark.gpu
 
@@ -52,13 +52,6 @@ SAMPLERS = [
     ("clamp_quad_f32", _abi.SAMPLER_CLAMP, _abi.STAGE_QUAD_F32, 0),
     ("clamp_quad_f16", _abi.SAMPLER_CLAMP, _abi.STAGE_QUAD_F16, 0),
 ]
-
-
-def gpu_view(sc, ids, dev, dmin, dmax, **kw):
-    imgs = torch.from_numpy(sc.images[ids].astype(np.float32)).to(dev)
-    cams = [engine.make_camera(*synthetic.camera_args(sc, i)) for i in ids]
-    return engine.ViewInputs(cams=cams, images=[imgs[k] for k in range(len(ids))], depth_min=dmin, depth_max=dmax,
-                             stream_id=ids[0], **kw)
 
 
 def mixed_hypotheses(sc, view, seed=1):
