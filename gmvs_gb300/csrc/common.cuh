@@ -63,6 +63,12 @@ struct DevParams {
     int pass_index, max_iterations;
     int nmax;  // largest N of the plan (shared-memory stride)
     float cost_thr[kMaxIters];
+    // The 8 x nmax neighbour-cost matrix of every pixel in flight lives in
+    // global memory (L2-resident), one block of 8 * nmax * 16 floats per
+    // resident warp: block (blockIdx.x * blockDim.y + threadIdx.y), element
+    // (k * nmax + i) * 16 + pixel-in-warp.  Keeping it out of shared memory
+    // lets more warps be resident.
+    float* ca;
 };
 
 // A tile is TW columns x TH thread rows of one view; thread row r covers

@@ -16,6 +16,7 @@ struct LaunchShape {
     size_t smem;   // dynamic shared memory bytes
     int sms = 1;   // SMs of the device (queue kernels: grid = resident CTAs)
     int ctas = 0;  // resident CTAs per SM wanted (0 = as many as fit)
+    int max_ctas = 0;  // resident CTAs per SM the plan's per-warp scratch holds (0 = no limit)
 };
 
 // One entry per variant, defined in pm_<variant>.cu.
@@ -44,6 +45,12 @@ cudaError_t launch_ncc_qf16(const LaunchShape&, const DevView*, const DevParams&
                             const float4*, float*, float*, uint32_t*, bool generic, cudaStream_t);
 cudaError_t launch_ncc_tex(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*,
                            const float4*, float*, float*, uint32_t*, bool generic, cudaStream_t);
+
+// Most CTAs of k_sweep that can be resident on one SM with this shape (0 on error).
+int sweep_ctas_per_sm_f32(const LaunchShape&, bool generic);
+int sweep_ctas_per_sm_qf32(const LaunchShape&, bool generic);
+int sweep_ctas_per_sm_qf16(const LaunchShape&, bool generic);
+int sweep_ctas_per_sm_tex(const LaunchShape&, bool generic);
 
 // Finalisation (runtime.cu): conversion, filter + export of one colour.
 cudaError_t launch_convert(const LaunchShape&, const DevView*, const Tile*, const int*, int final_buf, cudaStream_t);

@@ -562,7 +562,7 @@ __device__ void init_pixel(const DevView& V, const DevParams& prm, int px, int p
 // NCC loop.
 template <class S, int NS>
 __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int py, int iter, int colour, float* my,
-                            int npix, const Pair& q, float2* pw, int pstride) {
+                            int npix, const Pair& q, float2* pw, int pstride, float* __restrict__ ca) {
     const int W = V.W, H = V.H, N = V.N, nmax = prm.nmax;
     const int center = py * W + px;
     const int same = iter & 1;
@@ -573,11 +573,11 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
     const DevCam& rc = V.cam[0];
     const bool geom = V.sweep_kind == GMVS_SWEEP_GEOM;
     const bool prior_mode = V.sweep_kind == GMVS_SWEEP_PRIOR;
-#define CA(k, i) my[((k) * nmax + (i)) * npix]
-#define VW(i) my[(8 * nmax + (i)) * npix]
-#define POS(k) (*reinterpret_cast<int*>(&my[(9 * nmax + (k)) * npix]))
-#define FC(k) my[(9 * nmax + 8 + (k)) * npix]
-#define PL4(slot, c) my[(9 * nmax + 16 + 4 * (slot) + (c)) * npix]
+#define CA(k, i) ca[((k) * nmax + (i)) * 16]
+#define VW(i) my[(i) * npix]
+#define POS(k) (*reinterpret_cast<int*>(&my[(nmax + (k)) * npix]))
+#define FC(k) my[(nmax + 8 + (k)) * npix]
+#define PL4(slot, c) my[(nmax + 16 + 4 * (slot) + (c)) * npix]
 
     DevRng rng(prm.seed_lo, prm.seed_hi, (uint32_t)center, (uint32_t)V.stream_id,
                phase_of(V.pass_index, 1 + 2 * iter + colour));

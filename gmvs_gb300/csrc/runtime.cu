@@ -146,6 +146,8 @@ struct Layout {
     size_t tiles = 0;
     size_t images = 0;
     size_t state = 0;
+    size_t ca = 0;         // neighbour-cost scratch of the resident warps
+    int ca_ctas = 0;       // resident CTAs per SM it holds
     size_t total = 0;
     int ntiles = 0;
     std::vector<ImageSlot> slots;
@@ -225,6 +227,31 @@ int32_t validate(const gmvs_view_pass* views, int32_t n, const gmvs_params* p) {
 }
 
 
+int num_sms();
+
+// Block and dynamic shared memory of a plan's half-sweep kernel.
+LaunchShape sweep_shape(const gmvs_params* p, int nmax) {
+    const int TW = tile_w_of(p), TH = tile_h_of(p);
+    const size_t patch_bytes = (size_t)18 * (2 * TW * TH) * 8;  // kPatchSlots float2 per thread
+    return LaunchShape{1, dim3(2 * TW, TH), (size_t)(nmax + 28) * TW * TH * 4 + patch_bytes, num_sms(),
+                       p->ctas_per_sm, 0};
+}
+
+// Most resident CTAs per SM of that kernel (the neighbour-cost scratch is
+// sized for them); 64 warps per SM when the query fails.
+int sweep_max_ctas(int variant, const gmvs_params* p, int nmax) {
+    const LaunchShape ls = sweep_shape(p, nmax);
+    const bool generic = num_offsets(p) != 6;
+    int c = 0;
+    switch (variant) {
+        case kVarF32: c = sweep_ctas_per_sm_f32(ls, generic); break;
+        case kVarQuadF32: c = sweep_ctas_per_sm_qf32(ls, generic); break;
+        case kVarQuadF16: c = sweep_ctas_per_sm_qf16(ls, generic); break;
+        default: c = sweep_ctas_per_sm_tex(ls, generic); break;
+    }
+    return c > 0 ? c : 64 / tile_h_of(p);
+}
+
 Layout make_layout(const gmvs_view_pass* views, int32_t n, const gmvs_params* p, int variant, bool with_state) {
     Layout L;
     L.header = 256;
@@ -275,6 +302,12 @@ Layout make_layout(const gmvs_view_pass* views, int32_t n, const gmvs_params* p,
             off = align_up(off + px * 4 * 2);   // selected views
             off = align_up(off + px * 16);      // converted planes
         }
+        int nmax = 1;
+        for (int v = 0; v < n; ++v) nmax = std::max(nmax, views[v].num_src);
+        L.ca = off;
+        L.ca_ctas = sweep_max_ctas(variant, p, nmax);
+        const size_t warps = (size_t)num_sms() * L.ca_ctas * tile_h_of(p);
+        off = align_up(off + warps * 16 * 8 * nmax * sizeof(float));
     }
     L.total = off;
     return L;
@@ -469,6 +502,7 @@ int32_t build_plan(gmvs_plan* P, const gmvs_view_pass* views, int32_t n, const g
     int nmax = 1;
     for (int v = 0; v < n; ++v) nmax = std::max(nmax, views[v].num_src);
     fill_params(P->dprm, p, nmax);
+    if (with_state) P->dprm.ca = (float*)(P->ws + L.ca);
     P->slots = L.slots;
     int32_t rc = create_textures(P, L);
     if (rc != GMVS_OK) return rc;
@@ -519,7 +553,9 @@ int32_t build_plan(gmvs_plan* P, const gmvs_view_pass* views, int32_t n, const g
     const int sms = num_sms();
     const int ctas = p->ctas_per_sm;
     P->init_ls = LaunchShape{grid, dim3(2 * TW, TH), (size_t)2 * nmax * npix * 4 + patch_bytes, sms, ctas};
-    P->sweep_ls = LaunchShape{grid, dim3(2 * TW, TH), (size_t)(9 * nmax + 28) * npix * 4 + patch_bytes, sms, ctas};
+    P->sweep_ls = sweep_shape(p, nmax);
+    P->sweep_ls.grid = grid;
+    P->sweep_ls.max_ctas = with_state ? L.ca_ctas : 0;
     P->fin_ls = LaunchShape{grid, dim3(TW, TH), 0, sms, 0};
     P->num_stages = 2 * p->max_iterations + 4;
     P->final_buf = p->max_iterations & 1;

@@ -41,16 +41,28 @@ _PER_VIEW_BYTES = 4 + 72 + 20 + 16 + 1 + 8
 _PER_GEOM_PASS_VIEW_BYTES = 16
 # per reference view and pass: plane/cost/view-mask ping-pong + converted planes
 _PER_REF_PASS_BYTES = 64
+# per pass: the neighbour-cost scratch of every warp that can be resident
+# (at most 64 per SM), 16 pixels x 8 neighbours x num_src floats each
+_CA_BYTES_PER_WARP_SRC = 16 * 8 * 4
 _FIXED_BYTES = 64 << 20  # descriptors, tile lists, fusion scratch, allocator slack
 
 
-def footprint_bytes(num_views: int, height: int, width: int, num_refs: int, geom_iters: int = 2) -> int:
+def _num_sms() -> int:
+    if torch.cuda.is_available():
+        return torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    return 152  # GB300
+
+
+def footprint_bytes(num_views: int, height: int, width: int, num_refs: int, geom_iters: int = 2,
+                    max_src: int = 32, sms: Optional[int] = None) -> int:
     """Upper bound of the device memory one job holds while it is active."""
     px = height * width
     per_view = _PER_VIEW_BYTES + geom_iters * _PER_GEOM_PASS_VIEW_BYTES
     passes = 2 + geom_iters
     pitch_slack = 2 * num_views * height * 256  # texture rows padded to 256 bytes
-    return px * (num_views * per_view + num_refs * passes * _PER_REF_PASS_BYTES + 4) + pitch_slack + _FIXED_BYTES
+    ca = passes * (sms or _num_sms()) * 64 * _CA_BYTES_PER_WARP_SRC * max_src
+    return (px * (num_views * per_view + num_refs * passes * _PER_REF_PASS_BYTES + 4) + pitch_slack + ca +
+            _FIXED_BYTES)
 
 
 @dataclass
@@ -80,7 +92,8 @@ class Job:
 
     def footprint(self, geom_iters: int) -> int:
         V, H, W = self.images.shape
-        return footprint_bytes(V, H, W, len(self.problems), geom_iters)
+        max_src = max((len(s) for _, s in self.problems), default=1)
+        return footprint_bytes(V, H, W, len(self.problems), geom_iters, max_src)
 
 
 @dataclass

@@ -11,6 +11,10 @@ from gmvs_gb300 import _abi, engine
 from scenes import cam_args, gpu_view, gt_planes, random_planes
 
 COST_FP64_TOL = 1e-3   # stated bound of the fp32-accumulated cost against FP64
+# The texture sampler (module A) filters with the hardware's 8-bit fractional
+# weights; the FP64 oracle interpolates with exact weights, so its distance
+# to FP64 is the weight quantisation, not the arithmetic.
+TEX_FP64_TOL = 5e-3
 DEPTH_REL, NORMAL_DEG = 0.005, 1.0
 
 
@@ -43,7 +47,8 @@ def test_cost_error_against_fp64(gmvs_lib, orc, small, cuda, name, sampler, stag
     es = err[:, sample]
     print(f"\n{name}: |cost - FP64| on a 1% sample: max {es.max():.3e} mean {es.mean():.3e}; "
           f"all pixels: max {err.max():.3e} mean {err.mean():.3e} p99.9 {np.quantile(err, 0.999):.3e}")
-    assert es.max() <= COST_FP64_TOL and err.max() <= COST_FP64_TOL
+    tol = TEX_FP64_TOL if sampler == _abi.SAMPLER_TEX else COST_FP64_TOL
+    assert es.max() <= tol and err.max() <= tol
 
 
 @pytest.mark.gpu

@@ -79,10 +79,11 @@ def test_oversized_job_is_refused():
 
 def test_footprint_formula():
     # linear in the views and the reference views, positive fixed part
-    a = serving.footprint_bytes(10, 100, 100, 10)
-    b = serving.footprint_bytes(20, 100, 100, 20)
-    c = serving.footprint_bytes(0, 100, 100, 0)
+    a = serving.footprint_bytes(10, 100, 100, 10, max_src=4, sms=152)
+    b = serving.footprint_bytes(20, 100, 100, 20, max_src=4, sms=152)
+    c = serving.footprint_bytes(0, 100, 100, 0, max_src=4, sms=152)
     assert c > 0 and b - a == a - c
+    assert serving.footprint_bytes(10, 100, 100, 10, max_src=8, sms=152) > a
 
 
 def _scene_job(job_id, seed, H, W, arrival=0.0):
