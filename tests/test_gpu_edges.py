@@ -1,0 +1,89 @@
+"""CUDA path against the oracle, bit for bit, away from the default shape:
+the generic window path (window sizes and strides other than 11 / 2),
+image sizes that do not fill whole tiles, one source view, zero iterations,
+and one launch over views of uneven size and source count (the batching
+form) against one launch per view."""
+
+import numpy as np
+import pytest
+import torch
+
+from gmvs_gb300 import _abi, engine, synthetic
+from scenes import cam_args, gpu_view
+from test_gpu_parity import diff_report, same_bits
+
+pytestmark = pytest.mark.gpu
+
+
+def _pass(sc, ids, cuda, p):
+    v = gpu_view(sc, ids, cuda, 0.3, 6.0)
+    v.allocate_outputs(with_planes=True)
+    engine.run_passes([v], p, engine.Workspace())
+    return v.out_depth.cpu().numpy(), v.out_normal.cpu().numpy(), v.out_cost.cpu().numpy()
+
+
+def _oracle_pass(orc, sc, ids, **kw):
+    od, on, oc, _ = orc.run_pass(cam_args(sc, ids), sc.images[ids].astype(np.float32),
+                                 orc.make_params(depth_min=0.3, depth_max=6.0, stream_id=ids[0], **kw))
+    return od, on, oc
+
+
+def _check(g, o):
+    assert all(same_bits(a, b) for a, b in zip(g, o)), diff_report(depth=(g[0], o[0]), normal=(g[1], o[1]),
+                                                                   cost=(g[2], o[2]))
+
+
+@pytest.mark.parametrize("patch,stride,sampler", [(7, 1, _abi.SAMPLER_TEX), (11, 1, _abi.SAMPLER_CLAMP),
+                                                  (9, 2, _abi.SAMPLER_CLAMP), (5, 2, _abi.SAMPLER_TEX)])
+def test_generic_window_pass(gmvs_lib, orc, cuda, patch, stride, sampler):
+    sc = synthetic.small_scene(0, H=96, W=128)
+    ref, src = sc.problems[0]
+    ids = [ref] + src
+    p = engine.params_struct(sampler=sampler, staging=_abi.STAGE_F32, patch_size=patch, radius_increment=stride,
+                             max_iterations=2)
+    _check(_pass(sc, ids, cuda, p), _oracle_pass(orc, sc, ids, sampler=1 if sampler == _abi.SAMPLER_TEX else 0,
+                                                 patch_size=patch, radius_increment=stride, max_iterations=2))
+
+
+@pytest.mark.parametrize("H,W", [(67, 93), (33, 17), (130, 161)])
+def test_ragged_image_sizes(gmvs_lib, orc, cuda, H, W):
+    sc = synthetic.small_scene(1, H=H, W=W)
+    ref, src = sc.problems[0]
+    ids = [ref] + src
+    p = engine.params_struct(sampler=_abi.SAMPLER_CLAMP, staging=_abi.STAGE_QUAD_F16, max_iterations=2)
+    _check(_pass(sc, ids, cuda, p), _oracle_pass(orc, sc, ids, sampler=0, max_iterations=2))
+
+
+def test_one_source_and_zero_iterations(gmvs_lib, orc, cuda):
+    sc = synthetic.small_scene(2, H=64, W=80)
+    ref, src = sc.problems[0]
+    ids = [ref, src[0]]
+    p = engine.params_struct(sampler=_abi.SAMPLER_TEX, max_iterations=2)
+    _check(_pass(sc, ids, cuda, p), _oracle_pass(orc, sc, ids, sampler=1, max_iterations=2))
+    ids = [ref] + src
+    p = engine.params_struct(sampler=_abi.SAMPLER_TEX, max_iterations=0)
+    _check(_pass(sc, ids, cuda, p), _oracle_pass(orc, sc, ids, sampler=1, max_iterations=0))
+
+
+def test_uneven_batch_equals_single_launches(gmvs_lib, cuda):
+    """Views of different sizes and source counts in one launch per stage."""
+    scenes = [synthetic.small_scene(0, H=96, W=128), synthetic.small_scene(3, H=80, W=112),
+              synthetic.small_scene(4, H=120, W=96)]
+    picks = [(0, 4), (1, 2), (2, 3), (0, 1)]  # (scene, number of sources)
+    p = engine.params_struct(sampler=_abi.SAMPLER_CLAMP, staging=_abi.STAGE_QUAD_F16, max_iterations=2)
+    views, refs = [], []
+    for k, (si, n) in enumerate(picks):
+        sc = scenes[si]
+        ref, src = sc.problems[k % len(sc.problems)]
+        ids = [ref] + list(src)[:n]
+        refs.append((sc, ids))
+        views.append(gpu_view(sc, ids, cuda, 0.3, 6.0))
+        views[-1].allocate_outputs(with_planes=True)
+    engine.run_passes(views, p, engine.Workspace())
+    for v, (sc, ids) in zip(views, refs):
+        single = gpu_view(sc, ids, cuda, 0.3, 6.0)
+        single.allocate_outputs(with_planes=True)
+        engine.run_passes([single], p, engine.Workspace())
+        for a, b in ((single.out_depth, v.out_depth), (single.out_normal, v.out_normal),
+                     (single.out_planes, v.out_planes)):
+            assert torch.equal(torch.nan_to_num(a, 7.0), torch.nan_to_num(b, 7.0))
