@@ -164,6 +164,64 @@ def serving_run(dev) -> dict:
     return st
 
 
+def job_time_ms(ms: float, world: int, device) -> float:
+    """Whole-job step time: the slowest rank's (replicas run the same
+    workload, so the job ends with the last one)."""
+    import torch
+
+    if world <= 1:
+        return float(ms)
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def segments_run(dev) -> dict:
+    """The fusion scripts' superpixel statistics on one 1600x1200 view: the
+    device kernels (CUDA events, inputs resident) beside the host routine
+    that restates the reference's CPU code (one core)."""
+    import torch
+
+    from gmvs_gb300 import engine
+    from gmvs_gb300 import planar_initer as pi
+    from gmvs_gb300.synthetic import superpixel_case
+
+    rows, cols = 1200, 1600
+    seg, planar, n, var = superpixel_case(rows, cols, 1)
+    t = lambda a: torch.from_numpy(a).to(dev)
+    ds, dp, dn, dv = t(seg), t(planar), t(n), t(var)
+    ms_id = int(seg.max())
+    ws = engine.Workspace(dev)
+    out = {"size": f"{cols}x{rows}", "segments": ms_id}
+    for name, dev_fn, host_fn in (
+            ("fusion_planar_mask",
+             lambda: engine.fusion_planar_mask(ds, dp, dn, 100, max_seg_id=ms_id, workspace=ws),
+             lambda: pi.fusion_planar_mask(seg, planar, n, rows, cols, 100)),
+            ("filter_by_var_map",
+             lambda: engine.filter_by_var_map(dv, ds, 0.3, max_seg_id=ms_id, workspace=ws),
+             lambda: pi.filter_by_var_map(var, seg, 0.3)),
+            ("sliding_window_normal_7", lambda: engine.sliding_window_normal(dp, dn, 7),
+             lambda: pi.sliding_window_normal(planar, n, 7))):
+        for _ in range(3):
+            dev_fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            dev_fn()
+        e1.record()
+        torch.cuda.synchronize()
+        host_fn()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            host_fn()
+        host_ms = (time.perf_counter() - t0) / 3 * 1000.0
+        out[name] = {"device_ms": e0.elapsed_time(e1) / 10, "host_ms": host_ms}
+    return out
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
@@ -246,13 +304,7 @@ def main():
         e1.record()
         torch.cuda.synchronize()
     barrier()
-    ms = e0.elapsed_time(e1) / args.steps
-    t_max = torch.tensor([ms], device=dev)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
-    ms = float(t_max.item())
+    ms = job_time_ms(e0.elapsed_time(e1) / args.steps, world, dev)
     value = world * args.views / (ms / 1000.0)
 
     # per-stage breakdown and the dominant kernel's launch time (one instrumented step)
@@ -296,6 +348,7 @@ def main():
     served = None
     if not args.no_serving and rank == 0:
         served = serving_run(dev)
+    segments = segments_run(dev) if rank == 0 else None
 
     if rank != 0:
         return
@@ -332,6 +385,7 @@ def main():
                     {"p50_ms_per_view": ms / args.views, "p99_ms_per_view": ms / args.views,
                      "note": "batched: every view of the scene completes with the step"}),
         "serving": served,
+        "segments": segments,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
                      "kernel": "k_sweep (half-sweep over all views)", "peak_source": peak_note,

@@ -89,6 +89,12 @@ _SIGS = {
     "gmvs_fusion_planar_mask": (_i, [_p, _p, _p, _i, _i, _i, _f, _f, _f, _p]),
     "gmvs_filter_by_var_map": (_i, [_p, _p, _i, _i, _f, _p]),
     "gmvs_sliding_window_normal": (_i, [_p, _p, _i, _i, _i, _p]),
+    "gmvs_segments_workspace_bytes": (ctypes.c_size_t, [_i, _i, _i]),
+    "gmvs_fusion_planar_mask_device": (_i, [_p, _p, _p, _i, _i, _i, _i, _f, _f, _f, _p, _p, ctypes.c_size_t, _p]),
+    "gmvs_filter_by_var_map_device": (_i, [_p, _p, _i, _i, _i, _f, _p, _p, ctypes.c_size_t, _p]),
+    "gmvs_sliding_window_normal_device": (_i, [_p, _p, _i, _i, _i, _p, _p]),
+    "gmvs_gather_workspace_bytes": (ctypes.c_size_t, [_i, _i]),
+    "gmvs_gather_points": (_i, [_p, _p, _i, _i, _p, _p, _f, _p, _p, _p, _p, _p, _p, ctypes.c_size_t, _p]),
 }
 
 EXPORTED = tuple(_SIGS)

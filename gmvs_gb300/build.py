@@ -38,6 +38,8 @@ SOURCES = {
     "runtime.cu": [],
     "fusion.cu": [],
     "fuse_fixed.cu": [],
+    "segments.cu": [],
+    "gather.cu": [],
     "prior.cpp": [],
 }
 

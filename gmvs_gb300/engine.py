@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import ctypes
 from dataclasses import dataclass, field
-from typing import Optional, Sequence
+from typing import Optional, Sequence, Tuple
 
 import torch
 
@@ -275,3 +275,87 @@ def fuse(problem: gmvs_problem, cams: Sequence[gmvs_camera], depths: Sequence[to
     ptr, size = scratch.get(need)
     check(lib().gmvs_fuse(ctypes.byref(a), ptr, size, _abi.stream_ptr(stream)))
     return out_depth, out_normal
+
+
+# ------------------------------------------------ segment statistics (device)
+def _need_cuda(t: torch.Tensor, dtype, shape: tuple, name: str) -> None:
+    if not t.is_cuda or t.dtype != dtype or not t.is_contiguous() or tuple(t.shape) != shape:
+        raise ValueError(f"{name} must be a contiguous {dtype} CUDA tensor of shape {shape}")
+
+
+def _seg_workspace(rows: int, cols: int, max_seg: int, workspace: Optional[Workspace], dev) -> Tuple[int, int]:
+    need = lib().gmvs_segments_workspace_bytes(rows, cols, max_seg)
+    ws = workspace or Workspace(dev)
+    return ws.get(need) + (ws,)
+
+
+def fusion_planar_mask(seg_ids: torch.Tensor, planar_mask: torch.Tensor, normals: torch.Tensor, thresh: int = 100,
+                       nonplanar_percent: float = 0.75, cos_sim_thresh: float = 0.8, match_ratio_thresh: float = 0.9,
+                       max_seg_id: Optional[int] = None, workspace: Optional[Workspace] = None,
+                       stream: Optional[torch.cuda.Stream] = None) -> torch.Tensor:
+    """Device fusion_planar_mask: int32 [H, W] CUDA tensors in and out."""
+    rows, cols = int(seg_ids.shape[0]), int(seg_ids.shape[1])
+    _need_cuda(seg_ids, torch.int32, (rows, cols), "seg_ids")
+    _need_cuda(planar_mask, torch.int32, (rows, cols), "planar_mask")
+    _need_cuda(normals, torch.float32, (rows, cols, 3), "normals")
+    ms = int(seg_ids.max().item()) if max_seg_id is None else int(max_seg_id)
+    out = torch.empty((rows, cols), dtype=torch.int32, device=seg_ids.device)
+    ptr, size, _ws = _seg_workspace(rows, cols, max(ms, 0), workspace, seg_ids.device)
+    check(lib().gmvs_fusion_planar_mask_device(seg_ids.data_ptr(), planar_mask.data_ptr(), normals.data_ptr(), rows,
+                                               cols, max(ms, 0), int(thresh), float(nonplanar_percent),
+                                               float(cos_sim_thresh), float(match_ratio_thresh), out.data_ptr(), ptr,
+                                               size, _abi.stream_ptr(stream)))
+    return out
+
+
+def filter_by_var_map(var_map: torch.Tensor, seg_ids: torch.Tensor, var_thresh: float,
+                      max_seg_id: Optional[int] = None, workspace: Optional[Workspace] = None,
+                      stream: Optional[torch.cuda.Stream] = None) -> torch.Tensor:
+    """Device filter_by_var_map: float32 / int32 [H, W] CUDA tensors."""
+    rows, cols = int(var_map.shape[0]), int(var_map.shape[1])
+    _need_cuda(var_map, torch.float32, (rows, cols), "var_map")
+    _need_cuda(seg_ids, torch.int32, (rows, cols), "seg_ids")
+    ms = int(seg_ids.max().item()) if max_seg_id is None else int(max_seg_id)
+    out = torch.empty((rows, cols), dtype=torch.int32, device=seg_ids.device)
+    ptr, size, _ws = _seg_workspace(rows, cols, max(ms, 0), workspace, seg_ids.device)
+    check(lib().gmvs_filter_by_var_map_device(var_map.data_ptr(), seg_ids.data_ptr(), rows, cols, max(ms, 0),
+                                              float(var_thresh), out.data_ptr(), ptr, size, _abi.stream_ptr(stream)))
+    return out
+
+
+def sliding_window_normal(planar_region: torch.Tensor, normals: torch.Tensor, window_size: int,
+                          stream: Optional[torch.cuda.Stream] = None) -> torch.Tensor:
+    """Device sliding_window_normal: int32 [H, W] and float32 [H, W, 3] CUDA tensors."""
+    rows, cols = int(normals.shape[0]), int(normals.shape[1])
+    _need_cuda(planar_region, torch.int32, (rows, cols), "planar_region")
+    _need_cuda(normals, torch.float32, (rows, cols, 3), "normals")
+    out = torch.empty((rows, cols, 3), dtype=torch.float32, device=normals.device)
+    check(lib().gmvs_sliding_window_normal_device(planar_region.data_ptr(), normals.data_ptr(), rows, cols,
+                                                  int(window_size), out.data_ptr(), _abi.stream_ptr(stream)))
+    return out
+
+
+def gather_points(depth: torch.Tensor, normal: torch.Tensor, K, pose, cos_thresh: float,
+                  workspace: Optional[Workspace] = None, stream: Optional[torch.cuda.Stream] = None):
+    """World points of one view's fused maps (depth [H, W], normal [H, W, 3]
+    CUDA tensors; K 3x3, pose 4x4 camera-to-world).  Returns (points [M, 6],
+    facing points [M', 6], filtered depth [H, W], filtered normal [H, W, 3])."""
+    import numpy as np
+
+    H, W = int(depth.shape[0]), int(depth.shape[1])
+    _need_cuda(depth, torch.float32, (H, W), "depth")
+    _need_cuda(normal, torch.float32, (H, W, 3), "normal")
+    Kh = np.ascontiguousarray(np.asarray(K, np.float32).reshape(3, 3))
+    Ph = np.ascontiguousarray(np.asarray(pose, np.float32).reshape(4, 4))
+    dev = depth.device
+    pts = torch.empty((H * W, 6), dtype=torch.float32, device=dev)
+    fac = torch.empty((H * W, 6), dtype=torch.float32, device=dev)
+    od = torch.empty((H, W), dtype=torch.float32, device=dev)
+    on = torch.empty((H, W, 3), dtype=torch.float32, device=dev)
+    counts = (ctypes.c_int64 * 2)()
+    ws = workspace or Workspace(dev)
+    ptr, size = ws.get(lib().gmvs_gather_workspace_bytes(H, W))
+    check(lib().gmvs_gather_points(depth.data_ptr(), normal.data_ptr(), H, W, Kh.ctypes.data, Ph.ctypes.data,
+                                   float(cos_thresh), pts.data_ptr(), fac.data_ptr(), od.data_ptr(), on.data_ptr(),
+                                   ctypes.cast(counts, ctypes.c_void_p), ptr, size, _abi.stream_ptr(stream)))
+    return pts[: counts[0]], fac[: counts[1]], od, on

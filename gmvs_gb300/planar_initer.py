@@ -46,10 +46,21 @@ def _as_c(a: np.ndarray, dtype, shape, name: str) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=dtype)
 
 
+def _on_device(a) -> bool:
+    return getattr(a, "is_cuda", False) is True
+
+
 def fusion_planar_mask(seg_ids: np.ndarray, planar_mask: np.ndarray, normals: np.ndarray, rows: int, cols: int,
                        thresh: int = 100, nonplanar_percent: float = 0.75, cos_sim_thresh: float = 0.8,
                        match_ratio_thresh: float = 0.9) -> np.ndarray:
-    """fusion_planar_mask (planar_initer.cu:537-632)."""
+    """fusion_planar_mask (planar_initer.cu:537-632).  numpy arrays run the
+    host routine; CUDA tensors run the device kernels and return a CUDA
+    tensor (same values)."""
+    if _on_device(seg_ids):
+        from . import engine
+
+        return engine.fusion_planar_mask(seg_ids, planar_mask, normals, thresh, nonplanar_percent, cos_sim_thresh,
+                                         match_ratio_thresh)
     s = _as_c(seg_ids, np.int32, (rows, cols), "seg_ids")
     m = _as_c(planar_mask, np.int32, (rows, cols), "planar_mask")
     n = _as_c(normals, np.float32, (rows, cols, 3), "normals")
@@ -60,7 +71,12 @@ def fusion_planar_mask(seg_ids: np.ndarray, planar_mask: np.ndarray, normals: np
 
 
 def filter_by_var_map(var_map: np.ndarray, segment_ids_map: np.ndarray, var_thresh: float) -> np.ndarray:
-    """filter_by_var_map (planar_initer.cu:634-684)."""
+    """filter_by_var_map (planar_initer.cu:634-684); CUDA tensors run on the
+    device."""
+    if _on_device(var_map):
+        from . import engine
+
+        return engine.filter_by_var_map(var_map, segment_ids_map, var_thresh)
     v = np.ascontiguousarray(var_map, dtype=np.float32)
     rows, cols = v.shape
     s = _as_c(segment_ids_map, np.int32, (rows, cols), "segment_ids_map")
@@ -70,7 +86,12 @@ def filter_by_var_map(var_map: np.ndarray, segment_ids_map: np.ndarray, var_thre
 
 
 def sliding_window_normal(planar_region: np.ndarray, normal: np.ndarray, window_size: int) -> np.ndarray:
-    """sliding_window_normal (planar_initer.cu:471-535)."""
+    """sliding_window_normal (planar_initer.cu:471-535); CUDA tensors run on
+    the device."""
+    if _on_device(normal):
+        from . import engine
+
+        return engine.sliding_window_normal(planar_region, normal, window_size)
     n = np.ascontiguousarray(normal, dtype=np.float32)
     rows, cols = n.shape[:2]
     r = _as_c(planar_region, np.int32, (rows, cols), "planar_region")

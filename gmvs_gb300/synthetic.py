@@ -330,3 +330,32 @@ def write_scene(sc: Scene, root: str) -> None:
             for j in src:
                 f.write("%d %d " % (j, 100))
             f.write("\n")
+
+
+def superpixel_case(rows: int, cols: int, seed: int, cell=(24, 20)):
+    """Inputs of the fusion scripts' superpixel statistics: blocky superpixel
+    ids 1..K (1 % id-0 holes, gaps in the id range), a planar mask, unit
+    normals and a variance map.  Segments are drawn as textureless (10 %
+    non-planar pixels), objects (90 %, scattered normals), consistent
+    surfaces (90 %, one normal) or mixed (50 %), so every branch of
+    fusion_planar_mask is reached.  Returns (seg int32, planar int32,
+    normals float32 [rows, cols, 3], var float32)."""
+    rng = np.random.default_rng(seed)
+    ys, xs = np.mgrid[0:rows, 0:cols]
+    jy = rng.integers(0, cell[0], size=(rows // cell[0] + 2,))
+    gy = (ys + jy[np.minimum(xs // cell[1], len(jy) - 1)]) // cell[0]
+    gx = xs // cell[1]
+    seg = (gy * (cols // cell[1] + 2) + gx + 1).astype(np.int32)
+    seg[rng.random((rows, cols)) < 0.01] = 0
+    seg[seg % 17 == 0] = 0
+    ns = int(seg.max()) + 1
+    kind = rng.integers(0, 4, ns)
+    frac = np.array([0.1, 0.9, 0.9, 0.5])[kind]
+    planar = (rng.random((rows, cols)) >= frac[seg]).astype(np.int32)
+    base = rng.normal(size=(ns, 3))
+    base /= np.linalg.norm(base, axis=1, keepdims=True)
+    spread = np.where(kind == 1, 1.5, 0.05)[seg][..., None]
+    n = base[seg] + spread * rng.normal(size=(rows, cols, 3))
+    n = (n / np.linalg.norm(n, axis=-1, keepdims=True)).astype(np.float32)
+    var = rng.random((rows, cols)).astype(np.float32) * np.where(kind % 2 == 0, 0.4, 1.0)[seg].astype(np.float32)
+    return seg, planar, n, var

@@ -262,6 +262,52 @@ GMVS_API int32_t gmvs_sliding_window_normal(const int32_t* planar_region, const 
                                    int32_t rows, int32_t cols, int32_t window_size,
                                    float* out_normals);
 
+/* ------------------------------------------- device segment statistics --
+ * The three routines above on device arrays, with the same results bit for
+ * bit (every float sum in the reference's raster order).  Segment ids must
+ * lie in [0, max_seg_id] (the caller knows or computes the largest id);
+ * an id outside it is reported as GMVS_ERR_INVALID.  The two per-segment
+ * routines take a 256-byte aligned device workspace of
+ * gmvs_segments_workspace_bytes(rows, cols, max_seg_id) bytes and
+ * synchronise `stream` before returning (to read their error word). */
+GMVS_API size_t gmvs_segments_workspace_bytes(int32_t rows, int32_t cols, int32_t max_seg_id);
+/* planar_initer.cu:537-632 */
+GMVS_API int32_t gmvs_fusion_planar_mask_device(const int32_t* seg_ids, const int32_t* planar_mask,
+                                       const float* normals, int32_t rows, int32_t cols,
+                                       int32_t max_seg_id, int32_t thresh, float nonplanar_percent,
+                                       float cos_sim_thresh, float match_ratio_thresh,
+                                       int32_t* out_mask, void* workspace, size_t workspace_bytes,
+                                       void* stream);
+/* planar_initer.cu:634-684 */
+GMVS_API int32_t gmvs_filter_by_var_map_device(const float* var_map, const int32_t* seg_ids,
+                                      int32_t rows, int32_t cols, int32_t max_seg_id,
+                                      float var_thresh, int32_t* out_ids, void* workspace,
+                                      size_t workspace_bytes, void* stream);
+/* planar_initer.cu:471-535 */
+GMVS_API int32_t gmvs_sliding_window_normal_device(const int32_t* planar_region, const float* normals,
+                                          int32_t rows, int32_t cols, int32_t window_size,
+                                          float* out_normals, void* stream);
+
+/* ------------------------------------------------------------ point gather --
+ * The fusion scripts' gather of one view's fused depth/normal map into
+ * world points (gmvs/scripts/mvs_fusion_segmentaion.py:195-236), one device
+ * pass: for every pixel with depth > 0, p = o + depth * R d with
+ * d = ((x - cx) / fx, (y - cy) / fy, 1) and (R, o) the camera-to-world pose,
+ * written with its normal as 6 floats to out_points in raster order; the
+ * points with dot(-R d, n) > cos_thresh (normal facing the camera) also go
+ * to out_facing (optional), and out_depth / out_normal (optional) receive
+ * the maps with only those pixels kept.  depth [H][W], normal [H][W][3] and
+ * the outputs are device arrays; out_points and out_facing hold up to H * W
+ * points.  intrinsics: host 3x3 row-major K; pose: host 4x4 row-major.
+ * out_counts (host, 2 entries) receives the two point counts; the call
+ * synchronises `stream`.  No counterpart in the reference's C++ (it is
+ * torch code in the script). */
+GMVS_API size_t gmvs_gather_workspace_bytes(int32_t height, int32_t width);
+GMVS_API int32_t gmvs_gather_points(const float* depth, const float* normal, int32_t height, int32_t width,
+                           const float* intrinsics, const float* pose, float cos_thresh,
+                           float* out_points, float* out_facing, float* out_depth, float* out_normal,
+                           int64_t* out_counts, void* workspace, size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
