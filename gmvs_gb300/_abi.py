@@ -95,6 +95,7 @@ _SIGS = {
     "gmvs_sliding_window_normal_device": (_i, [_p, _p, _i, _i, _i, _p, _p]),
     "gmvs_gather_workspace_bytes": (ctypes.c_size_t, [_i, _i]),
     "gmvs_gather_points": (_i, [_p, _p, _i, _i, _p, _p, _f, _p, _p, _p, _p, _p, _p, ctypes.c_size_t, _p]),
+    "gmvs_view_scores": (_i, [_p, _p, _i, _p, _i, _p, _p, _p]),
 }
 
 EXPORTED = tuple(_SIGS)

@@ -40,6 +40,7 @@ SOURCES = {
     "fuse_fixed.cu": [],
     "segments.cu": [],
     "gather.cu": [],
+    "views.cu": [],
     "prior.cpp": [],
 }
 

@@ -308,6 +308,19 @@ GMVS_API int32_t gmvs_gather_points(const float* depth, const float* normal, int
                            float* out_points, float* out_facing, float* out_depth, float* out_normal,
                            int64_t* out_counts, void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---------------------------------------------------------- view selection --
+ * calc_score of the COLMAP conversion (gmvs/scripts/colmap2mvs.py:324-357)
+ * for every pair of num_images images, into the symmetric device matrix
+ * scores [V][V] (zero diagonal).  point_ids: device int32, image i's point
+ * ids sorted ascending without -1 entries at [offsets[i], offsets[i+1])
+ * (offsets: device, V + 1 entries); xyz: device FP64 [num_points][3] indexed
+ * by point id (ids outside it are ignored); centers: device FP64 [V][3]
+ * camera centres.  No counterpart in the reference's C++ (it is a Python
+ * loop over a process pool). */
+GMVS_API int32_t gmvs_view_scores(const long long* offsets, const int32_t* point_ids, int32_t num_images,
+                         const double* xyz, int32_t num_points, const double* centers, float* scores,
+                         void* stream);
+
 #ifdef __cplusplus
 }
 #endif
