@@ -87,8 +87,9 @@ class ScenePipeline:
         self.planes = [torch.empty((V, H, W, 4), **f32) for _ in range(2)]
         self.prior_planes = torch.empty((V, H, W, 4), **f32)
         self.prior_masks = torch.empty((V, H, W), dtype=torch.int32, device=dev)
-        self.fused_depth = torch.empty((V, H, W), **f32)
-        self.fused_normal = torch.empty((V, H, W, 3), **f32)
+        # zero for views that are no problem's reference (fusion writes the others)
+        self.fused_depth = torch.zeros((V, H, W), **f32)
+        self.fused_normal = torch.zeros((V, H, W, 3), **f32)
         self.masks = torch.zeros((V, H, W), dtype=torch.bool, device=dev)
         self.times = StageTimes()
         self.plans: Dict[str, List[Plan]] = {}

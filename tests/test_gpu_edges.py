@@ -87,3 +87,30 @@ def test_uneven_batch_equals_single_launches(gmvs_lib, cuda):
         for a, b in ((single.out_depth, v.out_depth), (single.out_normal, v.out_normal),
                      (single.out_planes, v.out_planes)):
             assert torch.equal(torch.nan_to_num(a, 7.0), torch.nan_to_num(b, 7.0))
+
+
+@pytest.mark.parametrize("scene", ["small", "room"])
+def test_staging_modes_agree(gmvs_lib, cuda, scene):
+    """fp32 rows, fp32 quads and fp16 quads hold the same taps of 8-bit
+    images, so whole geometric passes agree bit for bit."""
+    if scene == "small":
+        sc = synthetic.small_scene(0, H=128, W=160)
+    else:
+        sc = synthetic.room_scene(0, H=240, W=320, num_views=20, device=cuda)
+    ref, src = sc.problems[0]
+    ids = [ref] + list(src)
+    rng = np.random.default_rng(3)
+    d = (sc.depths * (1.0 + rng.normal(0, 0.005, sc.depths.shape))).astype(np.float32)
+    n = sc.normals + rng.normal(0, 0.02, sc.normals.shape)
+    n = (n / np.linalg.norm(n, axis=-1, keepdims=True)).astype(np.float32)
+    outs = []
+    for staging in (_abi.STAGE_F32, _abi.STAGE_QUAD_F32, _abi.STAGE_QUAD_F16):
+        p = engine.params_struct(sampler=_abi.SAMPLER_CLAMP, staging=staging, init_kind=_abi.INIT_DEPTH_NORMAL,
+                                 sweep_kind=_abi.SWEEP_GEOM, max_iterations=2, pass_index=2)
+        v = gpu_view(sc, ids, cuda, 0.3, 13.0, depths=[torch.from_numpy(d[i]).to(cuda) for i in ids],
+                     ref_normal=torch.from_numpy(n[ref]).to(cuda))
+        v.allocate_outputs(with_planes=True)
+        engine.run_passes([v], p, engine.Workspace())
+        outs.append((v.out_depth.cpu().numpy(), v.out_normal.cpu().numpy(), v.out_cost.cpu().numpy()))
+    for o in outs[1:]:
+        _check(o, outs[0])
