@@ -376,7 +376,9 @@ def main():
         "config": {"workload": WORKLOAD, "views": args.views, "height": args.height, "width": args.width,
                    "num_src": 10, "parallelism": f"replicas x{world}", "l2": "inputs larger than L2, no flush",
                    "cuda_graphs": True,
-                   "launch_shapes": {k: {"tile_h": r.best[0], "ctas_per_sm": r.best[1]} for k, r in pipe.tuned.items()}},
+                   "launch_shapes": {k: {"tile_h": r.best[0], "ctas_per_sm": r.best[1],
+                                         "split_sweep": r.best[2] if len(r.best) > 2 else 0}
+                                     for k, r in pipe.tuned.items()}},
         "e2e": {"value": world * args.views / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "latency": ({"p50_ms_per_view": served["p50_ms"], "p99_ms_per_view": served["p99_ms"],
@@ -423,7 +425,7 @@ def sweep_roofline(pipe, torch):
                     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                     a.record(stream)
                 plan.launch_stage(s)
-                launches += 1
+                launches += 2 if (is_sweep and plan.params.split_sweep) else 1  # split: two kernels
                 if is_sweep:
                     b.record(stream)
                     durations.append((a, b))

@@ -2,9 +2,12 @@
 
 The knobs that change speed but not results are the tile height (a tile is
 16 pixel columns by 2 * tile_h rows; tile_h thread rows of one warp each per
-CTA, so tile_h = 8 is a 16 x 16 tile and 4 a 16 x 8 tile) and the resident
+CTA, so tile_h = 8 is a 16 x 16 tile and 4 a 16 x 8 tile), the resident
 CTAs per SM (fewer CTAs leave more of the 256 KB of L1/shared memory to the
-sample cache, more CTAs hide more latency).  The window stride
+sample cache, more CTAs hide more latency) and whether each half-sweep runs
+as one kernel or as two (neighbour hypotheses, then view selection and
+refinement: fewer live registers per kernel, at the price of a per-pixel
+scratch in the workspace).  The window stride
 (radius_increment) is a parameter of the method -- stride 1 and 2 give
 different costs -- so it is not tuned: each stride is tuned on its own and
 keyed separately.
@@ -30,9 +33,13 @@ import torch
 from . import _abi
 from .engine import Plan, ViewInputs, Workspace
 
-TILE_HEIGHTS = (2, 4, 8)
-CTAS_PER_SM = (0, 3, 2)
-CANDIDATES: Tuple[Tuple[int, int], ...] = tuple((th, c) for th in TILE_HEIGHTS for c in CTAS_PER_SM)
+TILE_HEIGHTS = (4, 8)
+CTAS_PER_SM = (0, 3)
+SPLIT = (0, 1)
+# (tile_h, ctas_per_sm, split_sweep); 2-row tiles and 2 CTAs per SM never
+# won a sweep on the room scene (fewer resident warps) and are left out
+CANDIDATES: Tuple[Tuple[int, int, int], ...] = tuple(
+    (th, c, sp) for th in TILE_HEIGHTS for c in CTAS_PER_SM for sp in SPLIT)
 
 
 def _copy_params(p: _abi.gmvs_params) -> _abi.gmvs_params:
@@ -52,17 +59,18 @@ def tune_key(views: Sequence[ViewInputs], params: _abi.gmvs_params) -> str:
 @dataclass
 class TuneResult:
     key: str
-    best: Tuple[int, int]
-    ms: Dict[str, float] = field(default_factory=dict)  # "tile_h,ctas" -> ms per plan launch
+    best: Tuple[int, ...]
+    ms: Dict[str, float] = field(default_factory=dict)  # "tile_h,ctas,split" -> ms per plan launch
 
     def apply(self, params: _abi.gmvs_params) -> _abi.gmvs_params:
         q = _copy_params(params)
-        q.tile_h, q.ctas_per_sm = self.best
+        q.tile_h, q.ctas_per_sm = self.best[0], self.best[1]
+        q.split_sweep = self.best[2] if len(self.best) > 2 else 0
         return q
 
 
 class Autotuner:
-    def __init__(self, cache_path: Optional[str] = None, candidates: Sequence[Tuple[int, int]] = CANDIDATES,
+    def __init__(self, cache_path: Optional[str] = None, candidates: Sequence[Tuple[int, ...]] = CANDIDATES,
                  reps: int = 2, max_views: int = 2):
         self.cache_path = cache_path
         self.candidates = tuple(candidates)
@@ -85,7 +93,7 @@ class Autotuner:
 
     def tune(self, views: Sequence[ViewInputs], params: _abi.gmvs_params,
              stream: Optional[torch.cuda.Stream] = None) -> TuneResult:
-        """Best (tile_h, ctas_per_sm) for this kind of batch (cached)."""
+        """Best (tile_h, ctas_per_sm, split_sweep) for this kind of batch (cached)."""
         key = tune_key(views, params)
         if key in self.cache:
             return self.cache[key]
@@ -94,9 +102,11 @@ class Autotuner:
         st = stream or torch.cuda.current_stream(dev)
         ws = Workspace(dev)
         ms: Dict[str, float] = {}
-        for th, c in self.candidates:
+        for cand in self.candidates:
+            th, c = cand[0], cand[1]
+            sp = cand[2] if len(cand) > 2 else 0
             p = _copy_params(params)
-            p.tile_h, p.ctas_per_sm = th, c
+            p.tile_h, p.ctas_per_sm, p.split_sweep = th, c, sp
             plan = Plan(sample, p, ws, st)
             try:
                 plan.launch(st)  # warm-up (module load, first-touch)
@@ -106,7 +116,7 @@ class Autotuner:
                     plan.launch(st)
                 e1.record(st)
                 plan.check(st)
-                ms[f"{th},{c}"] = e0.elapsed_time(e1) / self.reps
+                ms[f"{th},{c},{sp}"] = e0.elapsed_time(e1) / self.reps
             finally:
                 plan.close()
         best = min(ms, key=ms.get)

@@ -69,6 +69,11 @@ struct DevParams {
     // (k * nmax + i) * 16 + pixel-in-warp.  Keeping it out of shared memory
     // lets more warps be resident.
     float* ca;
+    // Split half-sweeps (two kernels): the neighbour-cost matrix and the
+    // neighbour positions of every pixel of a launch, per work unit u (one
+    // thread row of a tile): nbc + u * 8 * nmax * 16, nbi + u * 10 * 16.
+    float* nbc;
+    int* nbi;
 };
 
 // A tile is TW columns x TH thread rows of one view; thread row r covers

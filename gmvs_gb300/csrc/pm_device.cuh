@@ -560,9 +560,15 @@ __device__ void init_pixel(const DevView& V, const DevParams& prm, int px, int p
 // positions, candidate final costs, refinement planes).  All 14 hypotheses
 // (8 neighbours, the current plane, 5 refinement candidates) go through one
 // NCC loop.
-template <class S, int NS>
+// PH selects the part of the half-sweep: 0 = all of it; 1 = the neighbour
+// hypotheses only (their cost matrix and positions go to per-pixel scratch);
+// 2 = the rest, from that scratch.  1 then 2 compute exactly what 0 does, as
+// two kernels with fewer live registers each.  `nb` (PH > 0): this pixel's
+// 10 scratch words (flags, same-colour bits, 8 positions) at stride 16.
+template <class S, int NS, int PH>
 __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int py, int iter, int colour, float* my,
-                            int npix, const Pair& q, float2* pw, int pstride, float* __restrict__ ca) {
+                            int npix, const Pair& q, float2* pw, int pstride, float* __restrict__ ca,
+                            int* __restrict__ nb) {
     const int W = V.W, H = V.H, N = V.N, nmax = prm.nmax;
     const int center = py * W + px;
     const int same = iter & 1;
@@ -590,8 +596,14 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
 
     // Adaptive checkerboard sampling.  pos = linear index; the buffer of a
     // candidate follows from its offset parity (odd = other colour).
-    int pos[8];
     unsigned flags = 0u, fromsame = 0u;
+    if constexpr (PH == 2) {
+        flags = (unsigned)nb[0];
+        fromsame = (unsigned)nb[16];
+        for (int k = 0; k < 8; ++k)
+            if ((flags >> k) & 1u) POS(k) = nb[(2 + k) * 16];
+    } else {
+    int pos[8];
     {
         float cmin;
         int cminp;
@@ -773,6 +785,14 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
     }
     for (int k = 0; k < 8; ++k)
         if ((flags >> k) & 1u) POS(k) = pos[k];
+    if constexpr (PH == 1) {
+        if (q.h == 0) {
+            nb[0] = (int)flags;
+            nb[16] = (int)fromsame;
+            for (int k = 0; k < 8; ++k) nb[(2 + k) * 16] = (flags >> k) & 1u ? pos[k] : 0;
+        }
+    }
+    }
 #define NPL(k) (V.plane[((fromsame >> (k)) & 1u) ? same : opp][POS(k)])
 
     // state carried between the phases of the hypothesis loop
@@ -786,7 +806,7 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
     const bool use_prior = prior_mode && mask > 0;
     int min_idx = 0;
 
-    for (int s = 0; s < 14; ++s) {
+    for (int s = PH == 2 ? 8 : 0; s < (PH == 1 ? 8 : 14); ++s) {
         float4 pl;
         const bool all_views = s < 8;
         if (s < 8) {
@@ -998,7 +1018,7 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
             }
         }
     }
-    if (q.h == 0) {
+    if (PH != 1 && q.h == 0) {
         V.plane[outb][center] = cur;
         V.cost[outb][center] = cur_cost;
         V.sel[outb][center] = cur_sel;

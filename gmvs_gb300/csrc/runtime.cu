@@ -147,6 +147,7 @@ struct Layout {
     size_t images = 0;
     size_t state = 0;
     size_t ca = 0;         // neighbour-cost scratch of the resident warps
+    size_t nbc = 0, nbi = 0;  // split half-sweeps: per-unit neighbour costs and positions
     int ca_ctas = 0;       // resident CTAs per SM it holds
     size_t total = 0;
     int ntiles = 0;
@@ -197,6 +198,7 @@ int32_t validate(const gmvs_view_pass* views, int32_t n, const gmvs_params* p) {
     if (p->tile_h < 0 || p->tile_h > 8) return fail(GMVS_ERR_INVALID, "tile_h must be in [0, 8]");
     if (p->tile_w != 0 && p->tile_w != 16) return fail(GMVS_ERR_INVALID, "tile_w must be 0 or 16");
     if (p->ctas_per_sm < 0 || p->ctas_per_sm > 32) return fail(GMVS_ERR_INVALID, "ctas_per_sm must be in [0, 32]");
+    if (p->split_sweep != 0 && p->split_sweep != 1) return fail(GMVS_ERR_INVALID, "split_sweep must be 0 or 1");
     for (int v = 0; v < n; ++v) {
         const gmvs_view_pass& V = views[v];
         if (V.height < 1 || V.width < 1) return fail(GMVS_ERR_INVALID, "view " + std::to_string(v) + ": empty image");
@@ -308,6 +310,13 @@ Layout make_layout(const gmvs_view_pass* views, int32_t n, const gmvs_params* p,
         L.ca_ctas = sweep_max_ctas(variant, p, nmax);
         const size_t warps = (size_t)num_sms() * L.ca_ctas * tile_h_of(p);
         off = align_up(off + warps * 16 * 8 * nmax * sizeof(float));
+        if (p->split_sweep) {
+            const size_t units = (size_t)ntiles * tile_h_of(p);
+            L.nbc = off;
+            off = align_up(off + units * 16 * 8 * nmax * sizeof(float));
+            L.nbi = off;
+            off = align_up(off + units * 16 * 10 * sizeof(int));
+        }
     }
     L.total = off;
     return L;
@@ -415,6 +424,7 @@ struct gmvs_plan {
     DevParams dprm;
     int variant = 0;
     bool generic = false;
+    bool split = false;   // half-sweeps as two kernels (gmvs_params.split_sweep)
     char* ws = nullptr;
     int* d_err = nullptr;
     int* d_ntiles = nullptr;  // tile queue: count, next unit, warps done
@@ -502,7 +512,14 @@ int32_t build_plan(gmvs_plan* P, const gmvs_view_pass* views, int32_t n, const g
     int nmax = 1;
     for (int v = 0; v < n; ++v) nmax = std::max(nmax, views[v].num_src);
     fill_params(P->dprm, p, nmax);
-    if (with_state) P->dprm.ca = (float*)(P->ws + L.ca);
+    if (with_state) {
+        P->dprm.ca = (float*)(P->ws + L.ca);
+        if (p->split_sweep) {
+            P->dprm.nbc = (float*)(P->ws + L.nbc);
+            P->dprm.nbi = (int*)(P->ws + L.nbi);
+        }
+    }
+    P->split = with_state && p->split_sweep != 0;
     P->slots = L.slots;
     int32_t rc = create_textures(P, L);
     if (rc != GMVS_OK) return rc;
@@ -611,14 +628,18 @@ int32_t launch_stage(gmvs_plan* P, int stage, cudaStream_t st) {
     } else if (stage <= 2 * I) {
         const int s = stage - 1;
         switch (P->variant) {
-            case kVarF32: e = launch_sweep_f32(P->sweep_ls, dv, P->dprm, dt, nt, s, P->d_err, P->generic, st); break;
+            case kVarF32:
+                e = launch_sweep_f32(P->sweep_ls, dv, P->dprm, dt, nt, s, P->d_err, P->generic, P->split, st);
+                break;
             case kVarQuadF32:
-                e = launch_sweep_qf32(P->sweep_ls, dv, P->dprm, dt, nt, s, P->d_err, P->generic, st);
+                e = launch_sweep_qf32(P->sweep_ls, dv, P->dprm, dt, nt, s, P->d_err, P->generic, P->split, st);
                 break;
             case kVarQuadF16:
-                e = launch_sweep_qf16(P->sweep_ls, dv, P->dprm, dt, nt, s, P->d_err, P->generic, st);
+                e = launch_sweep_qf16(P->sweep_ls, dv, P->dprm, dt, nt, s, P->d_err, P->generic, P->split, st);
                 break;
-            default: e = launch_sweep_tex(P->sweep_ls, dv, P->dprm, dt, nt, s, P->d_err, P->generic, st); break;
+            default:
+                e = launch_sweep_tex(P->sweep_ls, dv, P->dprm, dt, nt, s, P->d_err, P->generic, P->split, st);
+                break;
         }
     } else if (stage == 2 * I + 1) {
         e = launch_convert(P->fin_ls, dv, dt, nt, P->final_buf, st);

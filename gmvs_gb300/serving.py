@@ -61,7 +61,10 @@ def footprint_bytes(num_views: int, height: int, width: int, num_refs: int, geom
     passes = 2 + geom_iters
     pitch_slack = 2 * num_views * height * 256  # texture rows padded to 256 bytes
     ca = passes * (sms or _num_sms()) * 64 * _CA_BYTES_PER_WARP_SRC * max_src
-    return (px * (num_views * per_view + num_refs * passes * _PER_REF_PASS_BYTES + 4) + pitch_slack + ca +
+    # split half-sweeps (an autotuner choice): per pass and reference view,
+    # (8 * max_src + 10) words for every pixel of one colour, tiles rounded up
+    split = passes * num_refs * (width + 16) * (height + 16) // 2 * (8 * max_src + 10) * 4
+    return (px * (num_views * per_view + num_refs * passes * _PER_REF_PASS_BYTES + 4) + pitch_slack + ca + split +
             _FIXED_BYTES)
 
 

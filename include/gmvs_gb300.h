@@ -117,6 +117,9 @@ typedef struct gmvs_params {
     int32_t run_filter;       /* 1 = depth/normal conversion + checkerboard median filter */
     int32_t ctas_per_sm;      /* PatchMatch kernels: resident CTAs per SM (0 = as many as fit); fewer CTAs
                                  leave more of the SM's L1 to the texture/sample cache */
+    int32_t split_sweep;      /* 1 = each half-sweep as two kernels (neighbour hypotheses, then view
+                                 selection and refinement) through a per-pixel scratch in the workspace;
+                                 same results */
 } gmvs_params;
 
 /* One reference view of one pass.  All pointers are device pointers except

@@ -9,21 +9,22 @@ import pytest
 from gmvs_gb300 import _abi, autotune
 
 
-def test_candidates_cover_tile_shapes_and_residency():
-    assert {th for th, _ in autotune.CANDIDATES} == {2, 4, 8}  # 16x4, 16x8, 16x16 pixel tiles
-    assert {c for _, c in autotune.CANDIDATES} == {0, 2, 3}
+def test_candidates_cover_tile_shapes_residency_and_split():
+    assert {c[0] for c in autotune.CANDIDATES} == {4, 8}  # 16x8 and 16x16 pixel tiles
+    assert {c[1] for c in autotune.CANDIDATES} == {0, 3}
+    assert {c[2] for c in autotune.CANDIDATES} == {0, 1}
 
 
 def test_cache_file_round_trip(tmp_path, gmvs_lib):
     path = str(tmp_path / "tune.json")
     t = autotune.Autotuner(cache_path=path)
-    t.cache["k"] = autotune.TuneResult("k", (8, 3), {"8,3": 1.0, "4,0": 2.0})
+    t.cache["k"] = autotune.TuneResult("k", (8, 3, 1), {"8,3,1": 1.0, "4,0,0": 2.0})
     t._save()
     t2 = autotune.Autotuner(cache_path=path)
-    assert t2.cache["k"].best == (8, 3) and t2.cache["k"].ms["4,0"] == 2.0
+    assert t2.cache["k"].best == (8, 3, 1) and t2.cache["k"].ms["4,0,0"] == 2.0
     p = t2.cache["k"].apply(_abi.default_params())
-    assert (p.tile_h, p.ctas_per_sm) == (8, 3)
-    assert json.load(open(path))["k"]["best"] == [8, 3]
+    assert (p.tile_h, p.ctas_per_sm, p.split_sweep) == (8, 3, 1)
+    assert json.load(open(path))["k"]["best"] == [8, 3, 1]
 
 
 @pytest.mark.gpu
@@ -38,7 +39,8 @@ def test_launch_shape_does_not_change_results(gmvs_lib, small, cuda):
         for th, c in ((4, 0), (2, 3), (8, 2), (1, 1)):
             v = gpu_view(small, ids, cuda, 0.3, 6.0)
             v.allocate_outputs(with_planes=True)
-            p = engine.params_struct(sampler=sampler, staging=staging, tile_h=th, ctas_per_sm=c)
+            p = engine.params_struct(sampler=sampler, staging=staging, tile_h=th, ctas_per_sm=c,
+                                     split_sweep=int(th == 8))
             engine.run_passes([v], p, engine.Workspace())
             outs[(sampler, th, c)] = (v.out_depth.cpu().numpy(), v.out_cost.cpu().numpy(),
                                       v.out_planes.cpu().numpy())
@@ -58,7 +60,7 @@ def test_tuner_picks_a_candidate(gmvs_lib, small, cuda):
     ref, src = small.problems[0]
     v = gpu_view(small, [ref] + list(src), cuda, 0.3, 6.0)
     v.allocate_outputs()
-    t = autotune.Autotuner(candidates=((4, 0), (8, 0), (2, 3)), reps=1)
+    t = autotune.Autotuner(candidates=((4, 0, 0), (8, 0, 1), (2, 3, 0)), reps=1)
     r = t.tune([v], engine.params_struct())
-    assert r.best in ((4, 0), (8, 0), (2, 3)) and len(r.ms) == 3 and all(ms > 0 for ms in r.ms.values())
+    assert r.best in ((4, 0, 0), (8, 0, 1), (2, 3, 0)) and len(r.ms) == 3 and all(ms > 0 for ms in r.ms.values())
     assert t.tune([v], engine.params_struct()) is r  # cached

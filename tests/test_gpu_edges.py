@@ -114,3 +114,34 @@ def test_staging_modes_agree(gmvs_lib, cuda, scene):
         outs.append((v.out_depth.cpu().numpy(), v.out_normal.cpu().numpy(), v.out_cost.cpu().numpy()))
     for o in outs[1:]:
         _check(o, outs[0])
+
+
+@pytest.mark.parametrize("kind", ["random", "geom"])
+def test_split_half_sweeps_equal_single_kernel(gmvs_lib, cuda, kind):
+    """A half-sweep as two kernels (neighbour hypotheses, then the rest)
+    computes exactly what the single kernel does."""
+    sc = synthetic.small_scene(0, H=128, W=160)
+    views = [sc.problems[0], sc.problems[1]]
+    rng = np.random.default_rng(3)
+    d = (sc.depths * (1.0 + rng.normal(0, 0.005, sc.depths.shape))).astype(np.float32)
+    n = sc.normals + rng.normal(0, 0.02, sc.normals.shape)
+    n = (n / np.linalg.norm(n, axis=-1, keepdims=True)).astype(np.float32)
+    outs = []
+    for split in (0, 1):
+        if kind == "random":
+            p = engine.params_struct(sampler=_abi.SAMPLER_TEX, max_iterations=3, split_sweep=split)
+        else:
+            p = engine.params_struct(sampler=_abi.SAMPLER_CLAMP, init_kind=_abi.INIT_DEPTH_NORMAL,
+                                     sweep_kind=_abi.SWEEP_GEOM, max_iterations=2, pass_index=2, split_sweep=split)
+        vs = []
+        for ref, src in views:
+            ids = [ref] + list(src)
+            extra = {} if kind == "random" else dict(depths=[torch.from_numpy(d[i]).to(cuda) for i in ids],
+                                                      ref_normal=torch.from_numpy(n[ref]).to(cuda))
+            v = gpu_view(sc, ids, cuda, 0.3, 6.0, **extra)
+            v.allocate_outputs(with_planes=True)
+            vs.append(v)
+        engine.run_passes(vs, p, engine.Workspace())
+        outs.append([(v.out_depth.cpu().numpy(), v.out_normal.cpu().numpy(), v.out_cost.cpu().numpy()) for v in vs])
+    for a, b in zip(outs[0], outs[1]):
+        _check(b, a)
