@@ -45,7 +45,8 @@ class gmvs_params(ctypes.Structure):
                 ("disparity_max", _f), ("geom_consistency", _i), ("multi_geometry", _i), ("planar_prior", _i),
                 ("superpixel_filter", _i), ("seed", ctypes.c_uint64), ("init_kind", _i), ("sweep_kind", _i),
                 ("sampler", _i), ("staging", _i), ("pass_index", _i), ("tile_w", _i), ("tile_h", _i),
-                ("run_filter", _i), ("ctas_per_sm", _i), ("split_sweep", _i)]
+                ("run_filter", _i), ("ctas_per_sm", _i), ("split_sweep", _i),
+                ("tex_storage", _i)]
 
 
 class gmvs_view_pass(ctypes.Structure):

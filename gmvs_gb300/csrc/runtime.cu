@@ -166,7 +166,8 @@ int variant_of(const gmvs_params* p, int staging_resolved) {
     }
 }
 
-size_t bytes_per_pixel(int variant) {
+size_t bytes_per_pixel(int variant, const gmvs_params* p) {
+    if (variant == kVarTex && p->tex_storage == 1) return 0;  // CUDA arrays, outside the workspace
     switch (variant) {
         case kVarQuadF32: return 16;
         case kVarQuadF16: return 8;
@@ -199,6 +200,7 @@ int32_t validate(const gmvs_view_pass* views, int32_t n, const gmvs_params* p) {
     if (p->tile_w != 0 && p->tile_w != 16) return fail(GMVS_ERR_INVALID, "tile_w must be 0 or 16");
     if (p->ctas_per_sm < 0 || p->ctas_per_sm > 32) return fail(GMVS_ERR_INVALID, "ctas_per_sm must be in [0, 32]");
     if (p->split_sweep != 0 && p->split_sweep != 1) return fail(GMVS_ERR_INVALID, "split_sweep must be 0 or 1");
+    if (p->tex_storage != 0 && p->tex_storage != 1) return fail(GMVS_ERR_INVALID, "tex_storage must be 0 or 1");
     for (int v = 0; v < n; ++v) {
         const gmvs_view_pass& V = views[v];
         if (V.height < 1 || V.width < 1) return fail(GMVS_ERR_INVALID, "view " + std::to_string(v) + ": empty image");
@@ -271,7 +273,7 @@ Layout make_layout(const gmvs_view_pass* views, int32_t n, const gmvs_params* p,
     // unique images
     std::map<const float*, int> idx;
     L.view_slots.resize(n);
-    const size_t bpp = bytes_per_pixel(variant);
+    const size_t bpp = bytes_per_pixel(variant, p);
     L.images = off;
     for (int v = 0; v < n; ++v) {
         for (int i = 0; i <= views[v].num_src; ++i) {
@@ -432,6 +434,7 @@ struct gmvs_plan {
     Tile* d_tiles = nullptr;
     int ntiles = 0;
     std::vector<cudaTextureObject_t> texs;
+    std::vector<cudaArray_t> arrays;  // tex_storage == 1: one CUDA array per image slot
     std::vector<ImageSlot> slots;
     LaunchShape init_ls, sweep_ls, fin_ls;
     int num_stages = 0;
@@ -443,15 +446,26 @@ namespace {
 // Texture objects over the workspace copies (created once per plan).
 int32_t create_textures(gmvs_plan* P, const Layout& L) {
     if (P->variant != kVarTex) return GMVS_OK;
+    const bool arrays = P->params.tex_storage == 1;
     for (const ImageSlot& s : L.slots) {
         cudaResourceDesc rd;
         std::memset(&rd, 0, sizeof(rd));
-        rd.resType = cudaResourceTypePitch2D;
-        rd.res.pitch2D.devPtr = P->ws + s.offset;
-        rd.res.pitch2D.desc = cudaCreateChannelDesc<float>();
-        rd.res.pitch2D.width = s.W;
-        rd.res.pitch2D.height = s.H;
-        rd.res.pitch2D.pitchInBytes = s.pitch;
+        if (arrays) {  // the block-linear layout of module A's cudaMallocArray (planar_initer.cu:150-158)
+            const cudaChannelFormatDesc cd = cudaCreateChannelDesc<float>();
+            cudaArray_t a = nullptr;
+            cudaError_t e = cudaMallocArray(&a, &cd, s.W, s.H);
+            if (e != cudaSuccess) return fail_cuda(e, "allocating texture arrays");
+            P->arrays.push_back(a);
+            rd.resType = cudaResourceTypeArray;
+            rd.res.array.array = a;
+        } else {
+            rd.resType = cudaResourceTypePitch2D;
+            rd.res.pitch2D.devPtr = P->ws + s.offset;
+            rd.res.pitch2D.desc = cudaCreateChannelDesc<float>();
+            rd.res.pitch2D.width = s.W;
+            rd.res.pitch2D.height = s.H;
+            rd.res.pitch2D.pitchInBytes = s.pitch;
+        }
         cudaTextureDesc td;  // the reference's descriptor (planar_initer.cu:150-158)
         std::memset(&td, 0, sizeof(td));
         td.addressMode[0] = cudaAddressModeWrap;
@@ -470,6 +484,12 @@ int32_t create_textures(gmvs_plan* P, const Layout& L) {
 // Refresh the staged copies of the caller's images (every launch, so new
 // image contents are always seen; capturable in a CUDA graph).
 int32_t restage(const gmvs_plan* P, cudaStream_t st) {
+    for (size_t k = 0; k < P->arrays.size(); ++k) {
+        const ImageSlot& s = P->slots[k];
+        cudaError_t e = cudaMemcpy2DToArrayAsync(P->arrays[k], 0, 0, s.src, (size_t)s.W * 4, (size_t)s.W * 4, s.H,
+                                                 cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return fail_cuda(e, "staging texture arrays");
+    }
     for (const ImageSlot& s : P->slots) {
         if (s.offset == ~(size_t)0) continue;
         void* dst = P->ws + s.offset;
@@ -711,6 +731,7 @@ extern "C" int32_t gmvs_plan_check(gmvs_plan* plan, void* stream) {
 extern "C" void gmvs_plan_destroy(gmvs_plan* plan) {
     if (!plan) return;
     for (cudaTextureObject_t t : plan->texs) cudaDestroyTextureObject(t);
+    for (cudaArray_t a : plan->arrays) cudaFreeArray(a);
     delete plan;
 }
 
@@ -777,5 +798,7 @@ extern "C" int32_t gmvs_ncc_costs(const gmvs_view_pass* view, const gmvs_params*
     }
     for (cudaTextureObject_t t : P.texs) cudaDestroyTextureObject(t);
     P.texs.clear();
+    for (cudaArray_t a : P.arrays) cudaFreeArray(a);
+    P.arrays.clear();
     return rc;
 }

@@ -120,6 +120,10 @@ typedef struct gmvs_params {
     int32_t split_sweep;      /* 1 = each half-sweep as two kernels (neighbour hypotheses, then view
                                  selection and refinement) through a per-pixel scratch in the workspace;
                                  same results */
+    int32_t tex_storage;      /* TEX sampler: 0 = pitched rows in the workspace; 1 = CUDA arrays (the
+                                 block-linear layout module A uses), allocated by gmvs_plan_create and
+                                 freed by gmvs_plan_destroy -- the one case where the library allocates
+                                 device memory; same results */
 } gmvs_params;
 
 /* One reference view of one pass.  All pointers are device pointers except

@@ -67,19 +67,24 @@ def main(nviews: int = 4) -> None:
         engine.run_passes([v], p, ws)
     torch.cuda.synchronize()
     plain_s = time.perf_counter() - t0
-    vs = views()
-    plan = engine.Plan(vs, p, ws)
-    plan.launch()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    plan.launch()
-    plan.check()
-    batched_s = time.perf_counter() - t0
+    batched = {}
+    for split in (0, 1):
+        p.split_sweep = split
+        vs = views()
+        plan = engine.Plan(vs, p, engine.Workspace())
+        plan.launch()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        plan.launch()
+        plan.check()
+        batched[split] = time.perf_counter() - t0
+        plan.close()
     print(json.dumps({"views": len(problems), "size": "1600x1200", "num_src": len(problems[0][1]),
                       "reference_module_b_ms_per_view": 1000 * ref_s / len(problems),
                       "reference_breakdown_ms_per_view": {k: 1000 * v / len(problems) for k, v in ref_t.items()},
                       "gmvs_plain_ms_per_view": 1000 * plain_s / len(problems),
-                      "gmvs_batched_ms_per_view": 1000 * batched_s / len(problems)}))
+                      "gmvs_batched_ms_per_view": 1000 * batched[0] / len(problems),
+                      "gmvs_batched_split_ms_per_view": 1000 * batched[1] / len(problems)}))
 
 
 if __name__ == "__main__":

@@ -145,3 +145,14 @@ def test_split_half_sweeps_equal_single_kernel(gmvs_lib, cuda, kind):
         outs.append([(v.out_depth.cpu().numpy(), v.out_normal.cpu().numpy(), v.out_cost.cpu().numpy()) for v in vs])
     for a, b in zip(outs[0], outs[1]):
         _check(b, a)
+
+
+def test_texture_arrays_equal_pitched_textures(gmvs_lib, orc, cuda):
+    """Module A's CUDA-array textures filter exactly like the pitched ones."""
+    sc = synthetic.small_scene(0, H=96, W=128)
+    ref, src = sc.problems[0]
+    ids = [ref] + src
+    outs = [_pass(sc, ids, cuda, engine.params_struct(sampler=_abi.SAMPLER_TEX, max_iterations=2, tex_storage=t))
+            for t in (0, 1)]
+    _check(outs[1], outs[0])
+    _check(outs[1], _oracle_pass(orc, sc, ids, sampler=1, max_iterations=2))
