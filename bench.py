@@ -414,8 +414,8 @@ def sweep_roofline(pipe, torch):
     stream = torch.cuda.current_stream()
     V = pipe.V
     HW = pipe.H * pipe.W
-    for key in ("random", "prior", "geom0", "geom1"):
-        plans = pipe.plans.get(key, [])
+    for key in sorted(pipe.plans):
+        plans = pipe.plans[key]
         for plan in plans:
             n_st = plan.num_stages
             iters = (n_st - 4) // 2
@@ -430,7 +430,7 @@ def sweep_roofline(pipe, torch):
                     b.record(stream)
                     durations.append((a, b))
                     b_img = 2  # fp16 staged images (algorithmic 2 B/pixel)
-                    if key in ("random", "prior"):
+                    if key.startswith(("random", "prior")):
                         b_img = 4  # fp32 textures
                     per_view = 0
                     for v in plan.views:
@@ -442,7 +442,7 @@ def sweep_roofline(pipe, torch):
     # fusion launches 2 kernels per view; a geometric pass restages its
     # fp16 texel quads with one kernel per image at stage 0
     launches += 2 * V
-    launches += sum(V for key in ("geom0", "geom1") if pipe.plans.get(key))
+    launches += sum(V for key in pipe.plans if key.startswith("geom"))
     if not ms:
         return None, 0, launches
     return float(np.mean(ms)), float(np.mean(nbytes)), launches

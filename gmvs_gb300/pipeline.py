@@ -55,7 +55,7 @@ class ScenePipeline:
 
     def __init__(self, scene: SceneInputs, geom_iters: int = 2, geom_consistent: int = 3, mode: str = "batched",
                  staging: int = _abi.STAGE_AUTO, tile_h: int = 0, prior_threads: int = 8, params=None,
-                 graphs: bool = False, autotuner=None):
+                 graphs: bool = False, autotuner=None, overlap: bool = True):
         if mode not in ("batched", "plain"):
             raise ValueError("mode is 'batched' or 'plain'")
         if graphs and mode != "batched":
@@ -93,12 +93,23 @@ class ScenePipeline:
         self.masks = torch.zeros((V, H, W), dtype=torch.bool, device=dev)
         self.times = StageTimes()
         self.plans: Dict[str, List[Plan]] = {}
+        # Batched runs split the random and prior passes into two view groups
+        # so that one group's host triangulation overlaps the other's device
+        # work (results do not depend on the grouping).
+        n = len(scene.problems)
+        self.groups: List[List[int]] = [list(range(n))]
+        if mode == "batched" and overlap and n >= 2:
+            self.groups = [list(range(n // 2)), list(range(n // 2, n))]
+        self._pinned: Optional[Dict[str, torch.Tensor]] = None
+        self._copy_stream: Optional[torch.cuda.Stream] = None
 
     # ------------------------------------------------------------ passes --
-    def _views(self, kind: str, out: int, src_buf: Optional[int] = None) -> List[ViewInputs]:
+    def _views(self, kind: str, out: int, src_buf: Optional[int] = None,
+               group: Optional[List[int]] = None) -> List[ViewInputs]:
         sc = self.sc
         views = []
-        for ref, src in sc.problems:
+        problems = sc.problems if group is None else [sc.problems[k] for k in group]
+        for ref, src in problems:
             ids = [ref] + list(src)
             dmin, dmax = _range(sc.cams[ref])
             v = ViewInputs(cams=[sc.cams[i] for i in ids], images=[sc.images[i] for i in ids], depth_min=dmin,
@@ -132,11 +143,15 @@ class ScenePipeline:
         return p
 
     def _passes(self):
-        """(key, kind, output buffer, input buffer, pass index) of every pass."""
-        out = [("random", "random", 0, None, 0), ("prior", "prior", 1, 0, 1)]
+        """(key, kind, output buffer, input buffer, pass index, view group) of
+        every pass: the random and prior passes per view group, then the
+        geometric passes over all views."""
+        multi = len(self.groups) > 1
+        out = [(f"random{g}" if multi else "random", "random", 0, None, 0, grp) for g, grp in enumerate(self.groups)]
+        out += [(f"prior{g}" if multi else "prior", "prior", 1, 0, 1, grp) for g, grp in enumerate(self.groups)]
         buf = 1
         for g in range(self.geom_iters):
-            out.append((f"geom{g}", "geom", 1 - buf, buf, 2 + g))
+            out.append((f"geom{g}", "geom", 1 - buf, buf, 2 + g, None))
             buf = 1 - buf
         return out
 
@@ -148,19 +163,19 @@ class ScenePipeline:
         its first launch instead, when its inputs exist to tune on."""
         if self.mode != "batched":
             return
-        for key, kind, out, src_buf, pass_index in self._passes():
+        for key, kind, out, src_buf, pass_index, group in self._passes():
             if self.autotuner is not None:
                 from .autotune import tune_key
 
-                if tune_key(self._views(kind, out, src_buf), self._params(kind, pass_index)) \
+                if tune_key(self._views(kind, out, src_buf, group), self._params(kind, pass_index)) \
                         not in self.autotuner.cache:
                     continue
-            self._ensure(key, kind, out, src_buf, pass_index, stream)
+            self._ensure(key, kind, out, src_buf, pass_index, group, stream)
 
     def _ensure(self, key: str, kind: str, out: int, src_buf: Optional[int], pass_index: int,
-                stream: Optional[torch.cuda.Stream]) -> None:
+                group: Optional[List[int]], stream: Optional[torch.cuda.Stream]) -> None:
         if key not in self.plans:
-            views = self._views(kind, out, src_buf)
+            views = self._views(kind, out, src_buf, group)
             p = self._params(kind, pass_index)
             if self.autotuner is not None:
                 res = self.autotuner.tune(views, p, stream)
@@ -178,9 +193,9 @@ class ScenePipeline:
             self._graphs[key] = g
 
     def _run(self, key: str, kind: str, out: int, src_buf: Optional[int], pass_index: int,
-             stream: Optional[torch.cuda.Stream]) -> None:
+             group: Optional[List[int]], stream: Optional[torch.cuda.Stream]) -> None:
         if self.mode == "batched":
-            self._ensure(key, kind, out, src_buf, pass_index, stream)
+            self._ensure(key, kind, out, src_buf, pass_index, group, stream)
             if self.graphs:
                 with torch.cuda.stream(stream or torch.cuda.current_stream()):
                     self._graphs[key].replay()
@@ -191,7 +206,7 @@ class ScenePipeline:
         # plain: one plan per view, a synchronisation after every kernel
         p = self._params(kind, pass_index)
         ws = self.ws.setdefault(key, Workspace())
-        for v in self._views(kind, out, src_buf):
+        for v in self._views(kind, out, src_buf, group):
             plan = Plan([v], p, ws, stream)
             for s in range(plan.num_stages):
                 plan.launch_stage(s, stream)
@@ -249,29 +264,94 @@ class ScenePipeline:
             return time.perf_counter()
 
         t = time.perf_counter()
-        self.random_pass(stream)
-        t = mark("random_pass", t)
-        self._prior(0)
-        t = mark("triangulation", t)
-        self.prior_pass(stream)
-        t = mark("prior_pass", t)
+        if len(self.groups) > 1 and not timed:
+            self._random_prior_overlapped(stream)
+        else:
+            self.random_pass(stream)
+            t = mark("random_pass", t)
+            self._prior(0)
+            t = mark("triangulation", t)
+            self.prior_pass(stream)
+            t = mark("prior_pass", t)
         buf = self.geom_passes(stream)
         t = mark("geom_passes", t)
         self.fusion(buf, stream)
         mark("fusion", t)
         return self.fused_depth, self.fused_normal
 
+    def _random_prior_overlapped(self, stream: Optional[torch.cuda.Stream]) -> None:
+        """Random passes of both view groups back to back; each group's
+        depth/cost maps go to pinned host memory on a copy stream as soon as
+        its pass ends and are triangulated on the host while the device
+        works on the other group; each group's prior pass is enqueued as
+        soon as its priors are uploaded."""
+        st = stream or torch.cuda.current_stream()
+        if self._pinned is None:
+            V, H, W = self.V, self.H, self.W
+            pin = lambda *shape, dt=torch.float32: torch.empty(shape, dtype=dt, pin_memory=True)
+            self._pinned = {"depth": pin(V, H, W), "cost": pin(V, H, W), "planes": pin(V, H, W, 4),
+                            "masks": pin(V, H, W, dt=torch.int32)}
+            self._copy_stream = torch.cuda.Stream(device=self.sc.images.device)
+        hp, cs = self._pinned, self._copy_stream
+        passes = self._passes()
+        ng = len(self.groups)
+        done = []
+        for g in range(ng):
+            self._run(*passes[g], stream)
+            ev = torch.cuda.Event()
+            ev.record(st)
+            done.append(ev)
+        with ThreadPoolExecutor(1) as ex:
+            futs = []
+            for g, grp in enumerate(self.groups):
+                refs = [self.sc.problems[k][0] for k in grp]
+                cs.wait_event(done[g])
+                with torch.cuda.stream(cs):
+                    for r in refs:
+                        hp["depth"][r].copy_(self.depth[0][r], non_blocking=True)
+                        hp["cost"][r].copy_(self.cost[0][r], non_blocking=True)
+                cs.synchronize()
+                futs.append(ex.submit(self._triangulate_into, refs))
+            for g, grp in enumerate(self.groups):
+                futs[g].result()
+                with torch.cuda.stream(st):
+                    for k in grp:
+                        r = self.sc.problems[k][0]
+                        self.prior_planes[r].copy_(hp["planes"][r], non_blocking=True)
+                        self.prior_masks[r].copy_(hp["masks"][r], non_blocking=True)
+                self._run(*passes[ng + g], stream)
+
+    def _triangulate_into(self, refs: List[int]) -> None:
+        """Planar priors of `refs` from the pinned depth/cost maps into the
+        pinned plane/mask buffers."""
+        sc, hp = self.sc, self._pinned
+        depth, cost = hp["depth"].numpy(), hp["cost"].numpy()
+        planes, masks = hp["planes"].numpy(), hp["masks"].numpy().view(np.uint32)
+        spf = sc.superpixels is not None
+
+        def one(ref: int) -> None:
+            dmin, dmax = _range(sc.cams[ref])
+            pl, mk, _ = build_planar_prior(sc.cams[ref], depth[ref], cost[ref],
+                                           sc.superpixels[ref] if spf else None, spf, dmin, dmax)
+            planes[ref], masks[ref] = pl, mk
+
+        with ThreadPoolExecutor(self.prior_threads) as ex:
+            list(ex.map(one, refs))
+
     # the stages one at a time (for schedulers that interleave scenes)
     def random_pass(self, stream: Optional[torch.cuda.Stream] = None) -> None:
-        self._run(*self._passes()[0], stream)
+        for args in self._passes()[:len(self.groups)]:
+            self._run(*args, stream)
 
     def prior_pass(self, stream: Optional[torch.cuda.Stream] = None) -> None:
-        self._run(*self._passes()[1], stream)
+        ng = len(self.groups)
+        for args in self._passes()[ng:2 * ng]:
+            self._run(*args, stream)
 
     def geom_passes(self, stream: Optional[torch.cuda.Stream] = None) -> int:
         """Enqueue the geometric passes; returns the buffer holding the result."""
         buf = 1
-        for args in self._passes()[2:]:
+        for args in self._passes()[2 * len(self.groups):]:
             self._run(*args, stream)
             buf = args[2]
         return buf
