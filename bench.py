@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-view comparison step")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-serving", action="store_true", help="skip the served-stream latency measurement")
+    ap.add_argument("--split", action="store_true",
+                    help="with --profile: run every half-sweep as two kernels (neighbours, then the rest)")
     ap.add_argument("--ref-views", type=int, default=0,
                     help="with --profile: reconstruct only the first K reference views of the scene (a smaller case "
                          "for detailed ncu captures; the full scene is still rendered)")
@@ -279,8 +281,11 @@ def main():
     # batched form: one persistent launch per stage over all views, each
     # pass's launch chain replayed from a CUDA graph, launch shapes picked by
     # the autotuner during the first (untimed) run
+    import types
+
     pipe = ScenePipeline(inputs, mode="batched", prior_threads=min(16, os.cpu_count() or 1),
-                         graphs=not args.profile, autotuner=None if args.profile else Autotuner(reps=1, max_views=2))
+                         graphs=not args.profile, autotuner=None if args.profile else Autotuner(reps=1, max_views=2),
+                         params=types.SimpleNamespace(split_sweep=1) if (args.profile and args.split) else None)
     if args.profile:
         pipe.run()
         torch.cuda.synchronize()

@@ -603,195 +603,195 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
         for (int k = 0; k < 8; ++k)
             if ((flags >> k) & 1u) POS(k) = nb[(2 + k) * 16];
     } else {
-    int pos[8];
-    {
-        float cmin;
-        int cminp;
-        bool csame;
-        if (py > 2) {  // up_far (odd offsets only)
-            flags |= 1u << 1;
-            cminp = center - 3 * W;
-            cmin = co[cminp];
-            for (int i = 1; i < 11; ++i)
-                if (py > 2 + 2 * i) {
-                    const int t = center - 3 * W - 2 * i * W;
-                    const float v = co[t];
-                    if (v < cmin) {
-                        cmin = v;
-                        cminp = t;
+        int pos[8];
+        {
+            float cmin;
+            int cminp;
+            bool csame;
+            if (py > 2) {  // up_far (odd offsets only)
+                flags |= 1u << 1;
+                cminp = center - 3 * W;
+                cmin = co[cminp];
+                for (int i = 1; i < 11; ++i)
+                    if (py > 2 + 2 * i) {
+                        const int t = center - 3 * W - 2 * i * W;
+                        const float v = co[t];
+                        if (v < cmin) {
+                            cmin = v;
+                            cminp = t;
+                        }
                     }
-                }
-            pos[1] = cminp;
-        }
-        if (py < H - 3) {  // down_far
-            flags |= 1u << 3;
-            cminp = center + 3 * W;
-            cmin = co[cminp];
-            for (int i = 1; i < 11; ++i)
-                if (py < H - 3 - 2 * i) {
-                    const int t = center + 3 * W + 2 * i * W;
-                    const float v = co[t];
-                    if (v < cmin) {
-                        cmin = v;
-                        cminp = t;
-                    }
-                }
-            pos[3] = cminp;
-        }
-        if (px > 2) {  // left_far
-            flags |= 1u << 5;
-            cminp = center - 3;
-            cmin = co[cminp];
-            for (int i = 1; i < 11; ++i)
-                if (px > 2 + 2 * i) {
-                    const int t = center - 3 - 2 * i;
-                    const float v = co[t];
-                    if (v < cmin) {
-                        cmin = v;
-                        cminp = t;
-                    }
-                }
-            pos[5] = cminp;
-        }
-        if (px < W - 3) {  // right_far keeps the maximum (patch_match_kernel.cu:954)
-            flags |= 1u << 7;
-            cminp = center + 3;
-            cmin = co[cminp];
-            for (int i = 1; i < 11; ++i)
-                if (px < W - 3 - 2 * i) {
-                    const int t = center + 3 + 2 * i;
-                    const float v = co[t];
-                    if (cmin < v) {
-                        cmin = v;
-                        cminp = t;
-                    }
-                }
-            pos[7] = cminp;
-        }
-        // near neighbours: the first candidate (offset 1) has the other
-        // colour, the V-shaped ones (offset parity even) this colour.
-        if (py > 0) {  // up_near
-            flags |= 1u << 0;
-            cminp = center - W;
-            cmin = co[cminp];
-            csame = false;
-            for (int i = 0; i < 3; ++i) {
-                if (py > 1 + i && px > i) {
-                    const int t = center - W - (1 + i) * W - i;
-                    const float v = cs[t];
-                    if (v < cmin) {
-                        cmin = v;
-                        cminp = t;
-                        csame = true;
-                    }
-                }
-                if (py > 1 + i && px < W - 1 - i) {
-                    const int t = center - W - (1 + i) * W + i;
-                    const float v = cs[t];
-                    if (v < cmin) {
-                        cmin = v;
-                        cminp = t;
-                        csame = true;
-                    }
-                }
+                pos[1] = cminp;
             }
-            pos[0] = cminp;
-            if (csame) fromsame |= 1u << 0;
-        }
-        if (py < H - 1) {  // down_near
-            flags |= 1u << 2;
-            cminp = center + W;
-            cmin = co[cminp];
-            csame = false;
-            for (int i = 0; i < 3; ++i) {
-                if (py < H - 2 - i && px > i) {
-                    const int t = center + W + (1 + i) * W - i;
-                    const float v = cs[t];
-                    if (v < cmin) {
-                        cmin = v;
-                        cminp = t;
-                        csame = true;
+            if (py < H - 3) {  // down_far
+                flags |= 1u << 3;
+                cminp = center + 3 * W;
+                cmin = co[cminp];
+                for (int i = 1; i < 11; ++i)
+                    if (py < H - 3 - 2 * i) {
+                        const int t = center + 3 * W + 2 * i * W;
+                        const float v = co[t];
+                        if (v < cmin) {
+                            cmin = v;
+                            cminp = t;
+                        }
                     }
-                }
-                if (py < H - 2 - i && px < W - 1 - i) {
-                    const int t = center + W + (1 + i) * W + i;
-                    const float v = cs[t];
-                    if (v < cmin) {
-                        cmin = v;
-                        cminp = t;
-                        csame = true;
-                    }
-                }
+                pos[3] = cminp;
             }
-            pos[2] = cminp;
-            if (csame) fromsame |= 1u << 2;
-        }
-        if (px > 0) {  // left_near
-            flags |= 1u << 4;
-            cminp = center - 1;
-            cmin = co[cminp];
-            csame = false;
-            for (int i = 0; i < 3; ++i) {
-                if (px > 1 + i && py > i) {
-                    const int t = center - 1 - (1 + i) - i * W;
-                    const float v = cs[t];
-                    if (v < cmin) {
-                        cmin = v;
-                        cminp = t;
-                        csame = true;
+            if (px > 2) {  // left_far
+                flags |= 1u << 5;
+                cminp = center - 3;
+                cmin = co[cminp];
+                for (int i = 1; i < 11; ++i)
+                    if (px > 2 + 2 * i) {
+                        const int t = center - 3 - 2 * i;
+                        const float v = co[t];
+                        if (v < cmin) {
+                            cmin = v;
+                            cminp = t;
+                        }
                     }
-                }
-                if (px > 1 + i && py < H - 1 - i) {
-                    const int t = center - 1 - (1 + i) + i * W;
-                    const float v = cs[t];
-                    if (v < cmin) {
-                        cmin = v;
-                        cminp = t;
-                        csame = true;
-                    }
-                }
+                pos[5] = cminp;
             }
-            pos[4] = cminp;
-            if (csame) fromsame |= 1u << 4;
-        }
-        if (px < W - 1) {  // right_near
-            flags |= 1u << 6;
-            cminp = center + 1;
-            cmin = co[cminp];
-            csame = false;
-            for (int i = 0; i < 3; ++i) {
-                if (px < W - 2 - i && py > i) {
-                    const int t = center + 1 + (1 + i) - i * W;
-                    const float v = cs[t];
-                    if (v < cmin) {
-                        cmin = v;
-                        cminp = t;
-                        csame = true;
+            if (px < W - 3) {  // right_far keeps the maximum (patch_match_kernel.cu:954)
+                flags |= 1u << 7;
+                cminp = center + 3;
+                cmin = co[cminp];
+                for (int i = 1; i < 11; ++i)
+                    if (px < W - 3 - 2 * i) {
+                        const int t = center + 3 + 2 * i;
+                        const float v = co[t];
+                        if (cmin < v) {
+                            cmin = v;
+                            cminp = t;
+                        }
                     }
-                }
-                if (px < W - 2 - i && py < H - 1 - i) {
-                    const int t = center + 1 + (1 + i) + i * W;
-                    const float v = cs[t];
-                    if (v < cmin) {
-                        cmin = v;
-                        cminp = t;
-                        csame = true;
-                    }
-                }
+                pos[7] = cminp;
             }
-            pos[6] = cminp;
-            if (csame) fromsame |= 1u << 6;
+            // near neighbours: the first candidate (offset 1) has the other
+            // colour, the V-shaped ones (offset parity even) this colour.
+            if (py > 0) {  // up_near
+                flags |= 1u << 0;
+                cminp = center - W;
+                cmin = co[cminp];
+                csame = false;
+                for (int i = 0; i < 3; ++i) {
+                    if (py > 1 + i && px > i) {
+                        const int t = center - W - (1 + i) * W - i;
+                        const float v = cs[t];
+                        if (v < cmin) {
+                            cmin = v;
+                            cminp = t;
+                            csame = true;
+                        }
+                    }
+                    if (py > 1 + i && px < W - 1 - i) {
+                        const int t = center - W - (1 + i) * W + i;
+                        const float v = cs[t];
+                        if (v < cmin) {
+                            cmin = v;
+                            cminp = t;
+                            csame = true;
+                        }
+                    }
+                }
+                pos[0] = cminp;
+                if (csame) fromsame |= 1u << 0;
+            }
+            if (py < H - 1) {  // down_near
+                flags |= 1u << 2;
+                cminp = center + W;
+                cmin = co[cminp];
+                csame = false;
+                for (int i = 0; i < 3; ++i) {
+                    if (py < H - 2 - i && px > i) {
+                        const int t = center + W + (1 + i) * W - i;
+                        const float v = cs[t];
+                        if (v < cmin) {
+                            cmin = v;
+                            cminp = t;
+                            csame = true;
+                        }
+                    }
+                    if (py < H - 2 - i && px < W - 1 - i) {
+                        const int t = center + W + (1 + i) * W + i;
+                        const float v = cs[t];
+                        if (v < cmin) {
+                            cmin = v;
+                            cminp = t;
+                            csame = true;
+                        }
+                    }
+                }
+                pos[2] = cminp;
+                if (csame) fromsame |= 1u << 2;
+            }
+            if (px > 0) {  // left_near
+                flags |= 1u << 4;
+                cminp = center - 1;
+                cmin = co[cminp];
+                csame = false;
+                for (int i = 0; i < 3; ++i) {
+                    if (px > 1 + i && py > i) {
+                        const int t = center - 1 - (1 + i) - i * W;
+                        const float v = cs[t];
+                        if (v < cmin) {
+                            cmin = v;
+                            cminp = t;
+                            csame = true;
+                        }
+                    }
+                    if (px > 1 + i && py < H - 1 - i) {
+                        const int t = center - 1 - (1 + i) + i * W;
+                        const float v = cs[t];
+                        if (v < cmin) {
+                            cmin = v;
+                            cminp = t;
+                            csame = true;
+                        }
+                    }
+                }
+                pos[4] = cminp;
+                if (csame) fromsame |= 1u << 4;
+            }
+            if (px < W - 1) {  // right_near
+                flags |= 1u << 6;
+                cminp = center + 1;
+                cmin = co[cminp];
+                csame = false;
+                for (int i = 0; i < 3; ++i) {
+                    if (px < W - 2 - i && py > i) {
+                        const int t = center + 1 + (1 + i) - i * W;
+                        const float v = cs[t];
+                        if (v < cmin) {
+                            cmin = v;
+                            cminp = t;
+                            csame = true;
+                        }
+                    }
+                    if (px < W - 2 - i && py < H - 1 - i) {
+                        const int t = center + 1 + (1 + i) + i * W;
+                        const float v = cs[t];
+                        if (v < cmin) {
+                            cmin = v;
+                            cminp = t;
+                            csame = true;
+                        }
+                    }
+                }
+                pos[6] = cminp;
+                if (csame) fromsame |= 1u << 6;
+            }
         }
-    }
-    for (int k = 0; k < 8; ++k)
-        if ((flags >> k) & 1u) POS(k) = pos[k];
-    if constexpr (PH == 1) {
-        if (q.h == 0) {
-            nb[0] = (int)flags;
-            nb[16] = (int)fromsame;
-            for (int k = 0; k < 8; ++k) nb[(2 + k) * 16] = (flags >> k) & 1u ? pos[k] : 0;
+        for (int k = 0; k < 8; ++k)
+            if ((flags >> k) & 1u) POS(k) = pos[k];
+        if constexpr (PH == 1) {
+            if (q.h == 0) {
+                nb[0] = (int)flags;
+                nb[16] = (int)fromsame;
+                for (int k = 0; k < 8; ++k) nb[(2 + k) * 16] = (flags >> k) & 1u ? pos[k] : 0;
+            }
         }
-    }
     }
 #define NPL(k) (V.plane[((fromsame >> (k)) & 1u) ? same : opp][POS(k)])
 
