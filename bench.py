@@ -386,6 +386,8 @@ def main():
                                      for k, r in pipe.tuned.items()}},
         "e2e": {"value": world * args.views / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
+        # pixels x source views evaluated per second (H * W * N * ref-views/s)
+        "mpix_views_per_s": value * args.height * args.width * 10 / 1e6,
         "latency": ({"p50_ms_per_view": served["p50_ms"], "p99_ms_per_view": served["p99_ms"],
                      "note": "served Poisson stream (see serving): arrival to fused maps on the host, per view"}
                     if served else

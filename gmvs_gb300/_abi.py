@@ -67,6 +67,7 @@ class gmvs_fuse_view(ctypes.Structure):
 _SIGS = {
     "gmvs_version": (_i, []),
     "gmvs_last_error": (ctypes.c_char_p, []),
+    "gmvs_bounds_violations": (_i, [_i]),
     "gmvs_default_params": (None, [ctypes.POINTER(gmvs_params)]),
     "gmvs_plan_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(gmvs_view_pass), _i,
                                                     ctypes.POINTER(gmvs_params)]),

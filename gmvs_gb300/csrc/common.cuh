@@ -74,6 +74,8 @@ struct DevParams {
     // thread row of a tile): nbc + u * 8 * nmax * 16, nbi + u * 10 * 16.
     float* nbc;
     int* nbi;
+    int ca_slots;  // warp blocks in `ca`
+    int nb_units;  // unit blocks in `nbc` / `nbi`
 };
 
 // A tile is TW columns x TH thread rows of one view; thread row r covers
@@ -156,6 +158,29 @@ __device__ __forceinline__ void release_queue(int* q, unsigned lane) {
     }
 }
 
+// ---------------------------------------------------- bounds-checked build --
+// Built with -DGMVS_BOUNDS_CHECK, every gathered index (image taps, depth
+// taps, neighbour costs and planes, per-warp and per-pixel scratch) is
+// tested against its array: an index outside it raises a bit in this
+// module's violation word (read by gmvs_bounds_violations) and the access
+// reads element 0 instead.  Compute-sanitizer's stand-in; the normal build
+// compiles the checks away.
+#ifdef GMVS_BOUNDS_CHECK
+static __device__ unsigned int g_oob;
+__device__ __forceinline__ long long checked_index(long long i, long long n, unsigned bit) {
+    if (i < 0 || i >= n) {
+        atomicOr(&g_oob, bit);
+        return 0;
+    }
+    return i;
+}
+#define GMVS_IDX(i, n, bit) ((int)gmvs::checked_index((long long)(i), (long long)(n), (bit)))
+#else
+#define GMVS_IDX(i, n, bit) (i)
+#endif
+// violation bits
+enum : unsigned { kOobImage = 1, kOobDepth = 2, kOobNeighbour = 4, kOobScratch = 8 };
+
 // --------------------------------------------------------------- helpers --
 __device__ __forceinline__ float lerpf(float a, float b, float w) { return fmaf(w, b - a, a); }
 
@@ -167,8 +192,11 @@ __device__ __forceinline__ float bilinear_clamp(const float* __restrict__ img, f
     const float wd = u - (float)wl;
     const int hu = (hl == H - 1) ? hl : hl + 1;
     const int wu = (wl == W - 1) ? wl : wl + 1;
-    const float v0 = __ldg(img + hl * W + wl), v1 = __ldg(img + hl * W + wu);
-    const float v2 = __ldg(img + hu * W + wl), v3 = __ldg(img + hu * W + wu);
+    const int n = H * W;
+    const float v0 = __ldg(img + GMVS_IDX(hl * W + wl, n, kOobDepth));
+    const float v1 = __ldg(img + GMVS_IDX(hl * W + wu, n, kOobDepth));
+    const float v2 = __ldg(img + GMVS_IDX(hu * W + wl, n, kOobDepth));
+    const float v3 = __ldg(img + GMVS_IDX(hu * W + wu, n, kOobDepth));
     return lerpf(lerpf(v0, v1, wd), lerpf(v2, v3, wd), hd);
 }
 

@@ -46,6 +46,12 @@ cudaError_t launch_ncc_qf16(const LaunchShape&, const DevView*, const DevParams&
 cudaError_t launch_ncc_tex(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*,
                            const float4*, float*, float*, uint32_t*, bool generic, cudaStream_t);
 
+// Bounds-check violation bits of each variant's kernels (~0u: not a checked build).
+unsigned oob_read_f32(bool reset);
+unsigned oob_read_qf32(bool reset);
+unsigned oob_read_qf16(bool reset);
+unsigned oob_read_tex(bool reset);
+
 // Most CTAs of k_sweep that can be resident on one SM with this shape (0 on error).
 int sweep_ctas_per_sm_f32(const LaunchShape&, bool generic);
 int sweep_ctas_per_sm_qf32(const LaunchShape&, bool generic);

@@ -18,7 +18,7 @@ struct SampF32 {  // plain fp32 rows, four loads per sample
     const float* __restrict__ p;
     int H, W;
     __device__ __forceinline__ SampF32(const DevView& V, int img) : p((const float*)V.img[img]), H(V.H), W(V.W) {}
-    __device__ __forceinline__ float at(int x, int y) const { return __ldg(p + y * W + x); }
+    __device__ __forceinline__ float at(int x, int y) const { return __ldg(p + GMVS_IDX(y * W + x, H * W, kOobImage)); }
     __device__ __forceinline__ float sample(float u, float v) const { return bilinear_clamp(p, u, v, H, W); }
     static constexpr bool kTex = false;
 };
@@ -45,12 +45,14 @@ struct SampQuadF32 {
     int H, W;
     __device__ __forceinline__ SampQuadF32(const DevView& V, int img)
         : p((const float4*)V.img[img]), H(V.H), W(V.W) {}
-    __device__ __forceinline__ float at(int x, int y) const { return __ldg(&p[y * W + x]).x; }
+    __device__ __forceinline__ float at(int x, int y) const {
+        return __ldg(&p[GMVS_IDX(y * W + x, H * W, kOobImage)]).x;
+    }
     __device__ __forceinline__ float sample(float u, float v) const {
         int idx;
         float wd, hd;
         clamp_corner(u, v, H, W, idx, wd, hd);
-        const float4 q = __ldg(&p[idx]);
+        const float4 q = __ldg(&p[GMVS_IDX(idx, H * W, kOobImage)]);
         return lerpf(lerpf(q.x, q.y, wd), lerpf(q.z, q.w, wd), hd);
     }
     static constexpr bool kTex = false;
@@ -65,12 +67,14 @@ struct SampQuadF16 {
         __half2 h = *reinterpret_cast<__half2*>(&u);
         return __half22float2(h);
     }
-    __device__ __forceinline__ float at(int x, int y) const { return h2f(__ldg(&p[y * W + x]).x).x; }
+    __device__ __forceinline__ float at(int x, int y) const {
+        return h2f(__ldg(&p[GMVS_IDX(y * W + x, H * W, kOobImage)]).x).x;
+    }
     __device__ __forceinline__ float sample(float u, float v) const {
         int idx;
         float wd, hd;
         clamp_corner(u, v, H, W, idx, wd, hd);
-        const uint2 q = __ldg(&p[idx]);
+        const uint2 q = __ldg(&p[GMVS_IDX(idx, H * W, kOobImage)]);
         const float2 t = h2f(q.x), b = h2f(q.y);
         return lerpf(lerpf(t.x, t.y, wd), lerpf(b.x, b.y, wd), hd);
     }
@@ -611,11 +615,11 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
             if (py > 2) {  // up_far (odd offsets only)
                 flags |= 1u << 1;
                 cminp = center - 3 * W;
-                cmin = co[cminp];
+                cmin = co[GMVS_IDX(cminp, H * W, kOobNeighbour)];
                 for (int i = 1; i < 11; ++i)
                     if (py > 2 + 2 * i) {
                         const int t = center - 3 * W - 2 * i * W;
-                        const float v = co[t];
+                        const float v = co[GMVS_IDX(t, H * W, kOobNeighbour)];
                         if (v < cmin) {
                             cmin = v;
                             cminp = t;
@@ -626,11 +630,11 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
             if (py < H - 3) {  // down_far
                 flags |= 1u << 3;
                 cminp = center + 3 * W;
-                cmin = co[cminp];
+                cmin = co[GMVS_IDX(cminp, H * W, kOobNeighbour)];
                 for (int i = 1; i < 11; ++i)
                     if (py < H - 3 - 2 * i) {
                         const int t = center + 3 * W + 2 * i * W;
-                        const float v = co[t];
+                        const float v = co[GMVS_IDX(t, H * W, kOobNeighbour)];
                         if (v < cmin) {
                             cmin = v;
                             cminp = t;
@@ -641,11 +645,11 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
             if (px > 2) {  // left_far
                 flags |= 1u << 5;
                 cminp = center - 3;
-                cmin = co[cminp];
+                cmin = co[GMVS_IDX(cminp, H * W, kOobNeighbour)];
                 for (int i = 1; i < 11; ++i)
                     if (px > 2 + 2 * i) {
                         const int t = center - 3 - 2 * i;
-                        const float v = co[t];
+                        const float v = co[GMVS_IDX(t, H * W, kOobNeighbour)];
                         if (v < cmin) {
                             cmin = v;
                             cminp = t;
@@ -656,11 +660,11 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
             if (px < W - 3) {  // right_far keeps the maximum (patch_match_kernel.cu:954)
                 flags |= 1u << 7;
                 cminp = center + 3;
-                cmin = co[cminp];
+                cmin = co[GMVS_IDX(cminp, H * W, kOobNeighbour)];
                 for (int i = 1; i < 11; ++i)
                     if (px < W - 3 - 2 * i) {
                         const int t = center + 3 + 2 * i;
-                        const float v = co[t];
+                        const float v = co[GMVS_IDX(t, H * W, kOobNeighbour)];
                         if (cmin < v) {
                             cmin = v;
                             cminp = t;
@@ -673,12 +677,12 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
             if (py > 0) {  // up_near
                 flags |= 1u << 0;
                 cminp = center - W;
-                cmin = co[cminp];
+                cmin = co[GMVS_IDX(cminp, H * W, kOobNeighbour)];
                 csame = false;
                 for (int i = 0; i < 3; ++i) {
                     if (py > 1 + i && px > i) {
                         const int t = center - W - (1 + i) * W - i;
-                        const float v = cs[t];
+                        const float v = cs[GMVS_IDX(t, H * W, kOobNeighbour)];
                         if (v < cmin) {
                             cmin = v;
                             cminp = t;
@@ -687,7 +691,7 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
                     }
                     if (py > 1 + i && px < W - 1 - i) {
                         const int t = center - W - (1 + i) * W + i;
-                        const float v = cs[t];
+                        const float v = cs[GMVS_IDX(t, H * W, kOobNeighbour)];
                         if (v < cmin) {
                             cmin = v;
                             cminp = t;
@@ -701,12 +705,12 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
             if (py < H - 1) {  // down_near
                 flags |= 1u << 2;
                 cminp = center + W;
-                cmin = co[cminp];
+                cmin = co[GMVS_IDX(cminp, H * W, kOobNeighbour)];
                 csame = false;
                 for (int i = 0; i < 3; ++i) {
                     if (py < H - 2 - i && px > i) {
                         const int t = center + W + (1 + i) * W - i;
-                        const float v = cs[t];
+                        const float v = cs[GMVS_IDX(t, H * W, kOobNeighbour)];
                         if (v < cmin) {
                             cmin = v;
                             cminp = t;
@@ -715,7 +719,7 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
                     }
                     if (py < H - 2 - i && px < W - 1 - i) {
                         const int t = center + W + (1 + i) * W + i;
-                        const float v = cs[t];
+                        const float v = cs[GMVS_IDX(t, H * W, kOobNeighbour)];
                         if (v < cmin) {
                             cmin = v;
                             cminp = t;
@@ -729,12 +733,12 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
             if (px > 0) {  // left_near
                 flags |= 1u << 4;
                 cminp = center - 1;
-                cmin = co[cminp];
+                cmin = co[GMVS_IDX(cminp, H * W, kOobNeighbour)];
                 csame = false;
                 for (int i = 0; i < 3; ++i) {
                     if (px > 1 + i && py > i) {
                         const int t = center - 1 - (1 + i) - i * W;
-                        const float v = cs[t];
+                        const float v = cs[GMVS_IDX(t, H * W, kOobNeighbour)];
                         if (v < cmin) {
                             cmin = v;
                             cminp = t;
@@ -743,7 +747,7 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
                     }
                     if (px > 1 + i && py < H - 1 - i) {
                         const int t = center - 1 - (1 + i) + i * W;
-                        const float v = cs[t];
+                        const float v = cs[GMVS_IDX(t, H * W, kOobNeighbour)];
                         if (v < cmin) {
                             cmin = v;
                             cminp = t;
@@ -757,12 +761,12 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
             if (px < W - 1) {  // right_near
                 flags |= 1u << 6;
                 cminp = center + 1;
-                cmin = co[cminp];
+                cmin = co[GMVS_IDX(cminp, H * W, kOobNeighbour)];
                 csame = false;
                 for (int i = 0; i < 3; ++i) {
                     if (px < W - 2 - i && py > i) {
                         const int t = center + 1 + (1 + i) - i * W;
-                        const float v = cs[t];
+                        const float v = cs[GMVS_IDX(t, H * W, kOobNeighbour)];
                         if (v < cmin) {
                             cmin = v;
                             cminp = t;
@@ -771,7 +775,7 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
                     }
                     if (px < W - 2 - i && py < H - 1 - i) {
                         const int t = center + 1 + (1 + i) + i * W;
-                        const float v = cs[t];
+                        const float v = cs[GMVS_IDX(t, H * W, kOobNeighbour)];
                         if (v < cmin) {
                             cmin = v;
                             cminp = t;
@@ -793,7 +797,7 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
             }
         }
     }
-#define NPL(k) (V.plane[((fromsame >> (k)) & 1u) ? same : opp][POS(k)])
+#define NPL(k) (V.plane[((fromsame >> (k)) & 1u) ? same : opp][GMVS_IDX(POS(k), H * W, kOobNeighbour)])
 
     // state carried between the phases of the hypothesis loop
     float weight_norm = 0.0f, cost_now = 0.0f, cur_cost = 0.0f, depth_now = 0.0f, restricted_cost = 0.0f;
@@ -819,8 +823,11 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
         } else if (s == 8) {
             // multi-hypothesis joint view selection (patch_match_kernel.cu:1114-1176)
             const uint32_t* so = V.sel[opp];
-            const uint32_t nb_sel[4] = {(flags & 1u) ? so[center - W] : 0u, (flags & 4u) ? so[center + W] : 0u,
-                                        (flags & 16u) ? so[center - 1] : 0u, (flags & 64u) ? so[center + 1] : 0u};
+            const int HW = H * W;
+            const uint32_t nb_sel[4] = {(flags & 1u) ? so[GMVS_IDX(center - W, HW, kOobNeighbour)] : 0u,
+                                        (flags & 4u) ? so[GMVS_IDX(center + W, HW, kOobNeighbour)] : 0u,
+                                        (flags & 16u) ? so[GMVS_IDX(center - 1, HW, kOobNeighbour)] : 0u,
+                                        (flags & 64u) ? so[GMVS_IDX(center + 1, HW, kOobNeighbour)] : 0u};
             const float thr = prm.cost_thr[iter];
             const float fallback = pmath::expf_(thr * thr / (-0.32f));
             float prob_sum = 0.0f;

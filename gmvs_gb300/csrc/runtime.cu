@@ -30,6 +30,17 @@ int32_t fail_cuda(cudaError_t e, const char* what) {
 }  // namespace gmvs
 
 extern "C" int32_t gmvs_version(void) { return 1; }
+
+extern "C" int32_t gmvs_bounds_violations(int32_t reset) {
+    const unsigned v[4] = {gmvs::oob_read_f32(reset != 0), gmvs::oob_read_qf32(reset != 0),
+                           gmvs::oob_read_qf16(reset != 0), gmvs::oob_read_tex(reset != 0)};
+    unsigned all = 0;
+    for (unsigned x : v) {
+        if (x == ~0u) return -1;
+        all |= x;
+    }
+    return (int32_t)all;
+}
 extern "C" const char* gmvs_last_error(void) { return g_last_error.c_str(); }
 
 extern "C" void gmvs_default_params(gmvs_params* p) {
@@ -534,6 +545,8 @@ int32_t build_plan(gmvs_plan* P, const gmvs_view_pass* views, int32_t n, const g
     fill_params(P->dprm, p, nmax);
     if (with_state) {
         P->dprm.ca = (float*)(P->ws + L.ca);
+        P->dprm.ca_slots = num_sms() * L.ca_ctas * tile_h_of(p);
+        P->dprm.nb_units = p->split_sweep ? L.ntiles * tile_h_of(p) : 0;
         if (p->split_sweep) {
             P->dprm.nbc = (float*)(P->ws + L.nbc);
             P->dprm.nbi = (int*)(P->ws + L.nbi);

@@ -263,19 +263,32 @@ class ScenePipeline:
                 self.times.add(name, time.perf_counter() - t0)
             return time.perf_counter()
 
+        nvtx = torch.cuda.nvtx  # host ranges for profilers (nsys / ncu --nvtx)
         t = time.perf_counter()
         if len(self.groups) > 1 and not timed:
+            nvtx.range_push("random+triangulation+prior (overlapped)")
             self._random_prior_overlapped(stream)
+            nvtx.range_pop()
         else:
+            nvtx.range_push("random_pass")
             self.random_pass(stream)
+            nvtx.range_pop()
             t = mark("random_pass", t)
+            nvtx.range_push("triangulation")
             self._prior(0)
+            nvtx.range_pop()
             t = mark("triangulation", t)
+            nvtx.range_push("prior_pass")
             self.prior_pass(stream)
+            nvtx.range_pop()
             t = mark("prior_pass", t)
+        nvtx.range_push("geom_passes")
         buf = self.geom_passes(stream)
+        nvtx.range_pop()
         t = mark("geom_passes", t)
+        nvtx.range_push("fusion")
         self.fusion(buf, stream)
+        nvtx.range_pop()
         mark("fusion", t)
         return self.fused_depth, self.fused_normal
 

@@ -80,10 +80,12 @@ class Job:
     problems: list
     superpixels: Optional[np.ndarray] = None
     arrival: float = 0.0          # seconds on the server clock
+    output_dir: Optional[str] = None  # write {ref:04d}.npy [H, W, 4] (depth, normal) there, as consistency.py
     admitted: float = -1.0
     finished: float = -1.0
     result: Optional[tuple] = None
     error: Optional[BaseException] = None
+    written: Optional[Future] = None  # the output files, when output_dir is set
 
     @property
     def num_views(self) -> int:
@@ -93,10 +95,30 @@ class Job:
     def num_refs(self) -> int:
         return len(self.problems)
 
+    def validate(self) -> None:
+        """Reject malformed requests before they take a slot."""
+        if self.images.ndim != 3 or min(self.images.shape) < 1:
+            raise ValueError(f"job {self.job_id}: images must be [V, H, W]")
+        V = self.images.shape[0]
+        if len(self.cams) != V:
+            raise ValueError(f"job {self.job_id}: {len(self.cams)} cameras for {V} images")
+        if not self.problems:
+            raise ValueError(f"job {self.job_id}: no reference views")
+        for ref, src in self.problems:
+            ids = [ref] + list(src)
+            if not src or len(src) > 32 or min(ids) < 0 or max(ids) >= V or ref in src:
+                raise ValueError(f"job {self.job_id}: bad problem {ref} <- {list(src)}")
+        if self.superpixels is not None and tuple(self.superpixels.shape) != tuple(self.images.shape):
+            raise ValueError(f"job {self.job_id}: superpixels do not match the images")
+
     def footprint(self, geom_iters: int) -> int:
         V, H, W = self.images.shape
         max_src = max((len(s) for _, s in self.problems), default=1)
         return footprint_bytes(V, H, W, len(self.problems), geom_iters, max_src)
+
+
+class Cancelled(RuntimeError):
+    """The job was cancelled before it finished."""
 
 
 @dataclass
@@ -109,6 +131,7 @@ class _Active:
     event: Optional[torch.cuda.Event] = None
     host: Optional[Future] = None
     pinned: Dict[str, torch.Tensor] = field(default_factory=dict)
+    cancel: bool = False
 
 
 class ReconstructionServer:
@@ -132,6 +155,9 @@ class ReconstructionServer:
         self.done: List[Job] = []
         self.in_use = 0
         self.pool = ThreadPoolExecutor(max(1, prior_threads))
+        # one stream per slot, reused by the jobs that take the slot (the
+        # caching allocator reuses a stream's freed blocks for that stream)
+        self._free_streams: List[torch.cuda.Stream] = []
         self.prior_threads = prior_threads
         self.t0 = time.perf_counter()
         self._lock = threading.Lock()
@@ -143,6 +169,7 @@ class ReconstructionServer:
     # ----------------------------------------------------------- requests --
     def submit(self, job: Job) -> Job:
         """Queue a job; it is admitted once it has arrived and fits."""
+        job.validate()
         if job.footprint(self.geom_iters) > self.budget:
             raise ValueError(f"job {job.job_id} needs {job.footprint(self.geom_iters)} bytes, more than the "
                              f"server's whole budget of {self.budget}")
@@ -162,8 +189,26 @@ class ReconstructionServer:
             heapq.heappop(self.queue)
             self._start(job, need)
 
+    def cancel(self, job_id: int) -> bool:
+        """Cancel a queued or active job; an active one stops at its next
+        step boundary and returns its memory.  True if the job was found."""
+        with self._lock:
+            for k, (_, jid, job) in enumerate(self.queue):
+                if jid == job_id:
+                    self.queue.pop(k)
+                    heapq.heapify(self.queue)
+                    job.error = Cancelled(f"job {job_id} cancelled while queued")
+                    job.finished = self.now()
+                    self.done.append(job)
+                    return True
+        for a in self.active:
+            if a.job.job_id == job_id:
+                a.cancel = True
+                return True
+        return False
+
     def _start(self, job: Job, need: int) -> None:
-        st = torch.cuda.Stream(device=self.device)
+        st = self._free_streams.pop() if self._free_streams else torch.cuda.Stream(device=self.device)
         with torch.cuda.stream(st):
             host = torch.from_numpy(np.ascontiguousarray(job.images))
             imgs = host.pin_memory().to(self.device, non_blocking=True).to(torch.float32)
@@ -188,6 +233,10 @@ class ReconstructionServer:
             return False
         if a.host is not None and not a.host.done():
             return False
+        if a.cancel:  # nothing of the job is in flight now
+            a.job.error = Cancelled(f"job {a.job.job_id} cancelled")
+            a.job.finished = self.now()
+            return True
         p, st = a.pipe, a.stream
         if a.step == 0:  # random pass, then the depth/cost maps to the host
             p.random_pass(st)
@@ -217,12 +266,15 @@ class ReconstructionServer:
         else:
             a.job.result = (a.pinned["fd"].numpy().copy(), a.pinned["fn"].numpy().copy())
             a.job.finished = self.now()
+            if a.job.output_dir:
+                a.job.written = self.pool.submit(write_depth_normal, a.job)
             return True
         a.step += 1
         return False
 
     def _retire(self, a: _Active) -> None:
         a.pipe.close()
+        self._free_streams.append(a.stream)
         self.in_use -= a.bytes
         self.active.remove(a)
         self.done.append(a.job)
@@ -254,6 +306,22 @@ class ReconstructionServer:
             a.pipe.close()
         self.active.clear()
         self.pool.shutdown(wait=True)
+
+
+def write_depth_normal(job: Job) -> List[str]:
+    """The fused maps of every reference view as {ref:04d}.npy [H, W, 4]
+    float32 (depth, normal) in job.output_dir, the layout consistency.py
+    writes (gmvs/consistency.py:199-210)."""
+    import os
+
+    os.makedirs(job.output_dir, exist_ok=True)
+    fd, fn = job.result
+    paths = []
+    for ref, _ in job.problems:
+        path = os.path.join(job.output_dir, f"{int(ref):04d}.npy")
+        np.save(path, np.concatenate([fd[ref][..., None], fn[ref]], -1).astype(np.float32))
+        paths.append(path)
+    return paths
 
 
 def latency_stats(jobs: List[Job]) -> dict:

@@ -167,6 +167,11 @@ typedef struct gmvs_fuse_view {
 } gmvs_fuse_view;
 
 GMVS_API int32_t gmvs_version(void);
+/* Bounds-checked builds (-DGMVS_BOUNDS_CHECK): the OR of the violation bits
+ * the PatchMatch kernels raised since the last reset (1 image tap, 2 depth
+ * tap, 4 neighbour cost or plane, 8 scratch; 0 = none); -1 in normal
+ * builds.  No counterpart in the reference (it has no checks). */
+GMVS_API int32_t gmvs_bounds_violations(int32_t reset);
 GMVS_API const char* gmvs_last_error(void);
 
 /* Fill `p` with the reference defaults (PatchMatchParams(), data_structure.hpp:20-37). */

@@ -29,6 +29,10 @@ class _StandIn(serving.ReconstructionServer):
         self.active.append(serving._Active(job=job, pipe=None, stream=None, bytes=need))
 
     def _advance(self, a):
+        if a.cancel:
+            a.job.error = serving.Cancelled("cancelled")
+            a.job.finished = self.now()
+            return True
         a.step += 1
         if a.step >= self.steps:
             a.job.finished = self.now()
@@ -42,8 +46,42 @@ class _StandIn(serving.ReconstructionServer):
 
 
 def _job(i, V=5, H=64, W=80, arrival=0.0):
-    return serving.Job(job_id=i, images=np.zeros((V, H, W), np.uint8), cams=[], problems=[(0, [1, 2])] * V,
-                       arrival=arrival)
+    return serving.Job(job_id=i, images=np.zeros((V, H, W), np.uint8), cams=[None] * V,
+                       problems=[(0, [1, 2])] * V, arrival=arrival)
+
+
+def test_malformed_jobs_are_rejected_at_submission():
+    srv = _StandIn(memory_budget=1 << 40)
+    bad = [
+        serving.Job(0, np.zeros((5, 8), np.uint8), [None] * 5, [(0, [1])]),          # not [V, H, W]
+        serving.Job(1, np.zeros((5, 8, 8), np.uint8), [None] * 4, [(0, [1])]),       # a camera missing
+        serving.Job(2, np.zeros((5, 8, 8), np.uint8), [None] * 5, []),               # no reference view
+        serving.Job(3, np.zeros((5, 8, 8), np.uint8), [None] * 5, [(0, [5])]),       # source out of range
+        serving.Job(4, np.zeros((5, 8, 8), np.uint8), [None] * 5, [(0, [0, 1])]),    # reference among sources
+        serving.Job(5, np.zeros((5, 8, 8), np.uint8), [None] * 5, [(0, [])]),        # no source view
+        serving.Job(6, np.zeros((5, 8, 8), np.uint8), [None] * 5, [(0, [1])],
+                    superpixels=np.zeros((5, 4, 4), np.uint8)),                      # superpixels of another size
+    ]
+    for job in bad:
+        with pytest.raises(ValueError):
+            srv.submit(job)
+    assert not srv.queue
+    srv.close()
+
+
+def test_cancel_queued_and_active_jobs():
+    srv = _StandIn(memory_budget=1 << 40, max_active=1)
+    srv.steps = 4
+    for i in range(3):
+        srv.submit(_job(i))
+    srv.poll()                       # job 0 admitted and stepping
+    assert srv.cancel(2) and srv.cancel(0) and not srv.cancel(99)
+    done = srv.run(idle_sleep=0)
+    by_id = {j.job_id: j for j in done}
+    assert isinstance(by_id[0].error, serving.Cancelled) and isinstance(by_id[2].error, serving.Cancelled)
+    assert by_id[1].error is None and by_id[1].finished >= 0
+    assert srv.in_use == 0 and srv.order == [0, 1]
+    srv.close()
 
 
 def test_admission_by_footprint_and_arrival_order():
@@ -96,16 +134,23 @@ def _scene_job(job_id, seed, H, W, arrival=0.0):
 
 
 @pytest.mark.gpu
-def test_same_result_alone_in_mix_and_direct(gmvs_lib, cuda):
+def test_same_result_alone_in_mix_and_direct(gmvs_lib, cuda, tmp_path):
     from gmvs_gb300.pipeline import SceneInputs, ScenePipeline
 
     a = _scene_job(0, 0, 256, 320)
+    a.output_dir = str(tmp_path / "depth_normal")
     srv = serving.ReconstructionServer(device=cuda, max_active=1, prior_threads=4)
     srv.submit(a)
     srv.run()
     srv.close()
     assert a.error is None, a.error
     alone = a.result
+    # the reference's file layout: {ref:04d}.npy [H, W, 4] = (depth, normal)
+    paths = a.written.result()
+    assert len(paths) == a.num_refs
+    ref0 = a.problems[0][0]
+    saved = np.load(paths[0])
+    assert saved.shape == (256, 320, 4) and np.array_equal(saved[..., 0], alone[0][ref0])
 
     a2 = _scene_job(0, 0, 256, 320)
     mix = [a2, _scene_job(1, 1, 192, 256), _scene_job(2, 2, 256, 320, arrival=0.01)]
