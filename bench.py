@@ -148,14 +148,14 @@ def cpu_baseline(sc, threads: int):
 def serving_run(dev) -> dict:
     """A bounded served stream: 6 room-scene jobs of 8-12 views at 640x480 to
     1600x1200 with 4-10 sources, Poisson arrivals at 2 jobs/s, continuous
-    batching under the default memory budget."""
+    batching with two jobs in flight under the default memory budget."""
     import torch
 
     from gmvs_gb300 import serving
 
     jobs = serving.poisson_stream(6, 2.0, seed=5, views=(8, 12), src=(4, 10), device=dev)
     torch.cuda.synchronize()
-    srv = serving.ReconstructionServer(device=dev, max_active=4, prior_threads=min(16, os.cpu_count() or 1))
+    srv = serving.ReconstructionServer(device=dev, max_active=2, prior_threads=min(16, os.cpu_count() or 1))
     for j in jobs:
         srv.submit(j)
     srv.run()
