@@ -29,13 +29,16 @@ struct DevCam {  // world -> camera, as gmvs_camera without the extents
 //   g   = (n_x / fx, n_y / fy, n_z - n_x cx / fx - n_y cy / fy) / w,
 // which is ComputeHomography (patch_match_kernel.cu:262-360) re-associated;
 // A_j and b_j are formed once per view pair in FP64 and rounded once.
+// Per source view j, hs[j] packs A_j, b_j and the centre-test extents into
+// four 16-byte words (one vector load each):
+//   hs[j][0] = A0 A1 A2 A3,  hs[j][1] = A4 A5 A6 A7,  hs[j][2] = A8 b0 b1 b2,
+//   hs[j][3] = src width, src height, 0, 0.
 struct DevView {
     int H, W, N, stream_id;
     int init_kind, sweep_kind, pass_index;  // per view, so one launch can mix passes
     float depth_min, depth_max;
-    float src_w[kMaxNgb], src_h[kMaxNgb];  // centre test extents (camera width/height)
-    float A[kMaxNgb][9];
-    float b[kMaxNgb][3];
+    int pad_[3];
+    float4 hs[kMaxNgb][4];
     DevCam cam[1 + kMaxNgb];  // ref, then sources (geometric term, conversions)
     const void* img[1 + kMaxNgb];           // CLAMP sampler: staged planes
     unsigned long long tex[1 + kMaxNgb];    // TEX sampler: texture objects

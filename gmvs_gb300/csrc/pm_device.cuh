@@ -226,8 +226,9 @@ __device__ __forceinline__ Hyp make_hyp(const DevCam& rc, float4 pl) {
 template <class S, int NS>
 __device__ __forceinline__ float ncc_cost(const DevView& V, const DevParams& prm, int j, const Hyp& h,
                                           const Patch<NS>& P, int px, int py, const Pair& q) {
-    const float* A = V.A[j];
-    const float* b = V.b[j];
+    const float4 h0 = V.hs[j][0], h1 = V.hs[j][1], h2 = V.hs[j][2], h3 = V.hs[j][3];
+    const float A[9] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w, h2.x};
+    const float b[3] = {h2.y, h2.z, h2.w};
     const float m0 = fmaf(-b[0], h.g0, A[0]), m1 = fmaf(-b[0], h.g1, A[1]), m2 = fmaf(-b[0], h.g2, A[2]);
     const float m3 = fmaf(-b[1], h.g0, A[3]), m4 = fmaf(-b[1], h.g1, A[4]), m5 = fmaf(-b[1], h.g2, A[5]);
     const float m6 = fmaf(-b[2], h.g0, A[6]), m7 = fmaf(-b[2], h.g1, A[7]), m8 = fmaf(-b[2], h.g2, A[8]);
@@ -235,7 +236,7 @@ __device__ __forceinline__ float ncc_cost(const DevView& V, const DevParams& prm
     const float cz = m6 * fpx + m7 * fpy + m8;
     const float cu = (m0 * fpx + m1 * fpy + m2) / cz;
     const float cv = (m3 * fpx + m4 * fpy + m5) / cz;
-    if (cu >= V.src_w[j] || cu < 0.0f || cv >= V.src_h[j] || cv < 0.0f) return 2.0f;
+    if (cu >= h3.x || cu < 0.0f || cv >= h3.y || cv < 0.0f) return 2.0f;
     const S src(V, j + 1);
     float ss = 0.f, sss = 0.f, srs = 0.f;
     if constexpr (NS > 0) {

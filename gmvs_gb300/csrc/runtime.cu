@@ -377,14 +377,17 @@ void fill_view(DevView& D, const gmvs_view_pass& V, const gmvs_params* p) {
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b)
                 KR[a * 3 + b] = Ks[a * 3 + 0] * Rr[0 * 3 + b] + Ks[a * 3 + 1] * Rr[1 * 3 + b] + Ks[a * 3 + 2] * Rr[2 * 3 + b];
+        float A[9], bv[3];
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b)
-                D.A[j][a * 3 + b] = (float)(KR[a * 3 + 0] * Kinv[0 * 3 + b] + KR[a * 3 + 1] * Kinv[1 * 3 + b] +
-                                            KR[a * 3 + 2] * Kinv[2 * 3 + b]);
+                A[a * 3 + b] = (float)(KR[a * 3 + 0] * Kinv[0 * 3 + b] + KR[a * 3 + 1] * Kinv[1 * 3 + b] +
+                                       KR[a * 3 + 2] * Kinv[2 * 3 + b]);
         for (int a = 0; a < 3; ++a)
-            D.b[j][a] = (float)(Ks[a * 3 + 0] * tr[0] + Ks[a * 3 + 1] * tr[1] + Ks[a * 3 + 2] * tr[2]);
-        D.src_w[j] = (float)s.width;
-        D.src_h[j] = (float)s.height;
+            bv[a] = (float)(Ks[a * 3 + 0] * tr[0] + Ks[a * 3 + 1] * tr[1] + Ks[a * 3 + 2] * tr[2]);
+        D.hs[j][0] = make_float4(A[0], A[1], A[2], A[3]);
+        D.hs[j][1] = make_float4(A[4], A[5], A[6], A[7]);
+        D.hs[j][2] = make_float4(A[8], bv[0], bv[1], bv[2]);
+        D.hs[j][3] = make_float4((float)s.width, (float)s.height, 0.0f, 0.0f);
     }
     D.ref_normal = V.ref_normal;
     D.prior_planes = (const float4*)V.prior_planes;
