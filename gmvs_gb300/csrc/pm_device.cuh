@@ -411,15 +411,24 @@ static __device__ __noinline__ float4 perturbed_normal(const DevCam& c, int px, 
     return np;
 }
 
-// compute_geom_consistency_cost (gmvs/src/patch_match.cu:562-593)
-static __device__ __noinline__ float geom_cost(const DevView& V, int j, float4 pl, int px, int py) {
+// compute_geom_consistency_cost (gmvs/src/patch_match.cu:562-593), in two
+// parts: the world point of the reference pixel at the plane's depth depends
+// only on the plane, so callers that test one plane against several source
+// views form it once (geom_point) and evaluate each view from it (geom_cost).
+struct GeomPoint {
+    float X[3];
+};
+__device__ __forceinline__ GeomPoint geom_point(const DevView& V, float4 pl, int px, int py) {
+    const DevCam& rc = V.cam[0];
+    GeomPoint g;
+    point_on_world((float)px, (float)py, depth_from_plane(rc, pl, px, py), rc, g.X);
+    return g;
+}
+static __device__ __noinline__ float geom_cost(const DevView& V, int j, const GeomPoint& g, int px, int py) {
     const DevCam& rc = V.cam[0];
     const DevCam& sc = V.cam[j + 1];
-    const float depth = depth_from_plane(rc, pl, px, py);
-    float X[3];
-    point_on_world((float)px, (float)py, depth, rc, X);
     float su, sv, sd;
-    project_on_camera(X, sc, su, sv, sd);
+    project_on_camera(g.X, sc, su, sv, sd);
     const float src_depth = bilinear_clamp(V.dep[j + 1], su, sv, V.H, V.W);
     if (src_depth == 0.0f) return 5.0f;
     float Y[3];
@@ -886,11 +895,13 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
             for (int k = 0; k < 8; ++k) {
                 float acc = 0.0f;
                 const bool fk = (flags >> k) & 1u;
+                GeomPoint gk;
+                if (geom && fk) gk = geom_point(V, NPL(k), px, py);
                 for (int j = 0; j < N; ++j) {
                     const float w = VW(j);
                     if (w > 0) {
                         if (geom && fk)
-                            acc += w * (CA(k, j) + 0.1f * geom_cost(V, j, NPL(k), px, py));
+                            acc += w * (CA(k, j) + 0.1f * geom_cost(V, j, gk, px, py));
                         else
                             acc += w * CA(k, j);
                     }
@@ -989,6 +1000,8 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
         // the hypothesis against every source view (neighbours) or the
         // sampled ones (current plane, refinement)
         const Hyp hy = make_hyp(rc, pl);
+        GeomPoint gp;
+        if (geom && !all_views) gp = geom_point(V, pl, px, py);
         float acc = 0.0f;
         for (int j = 0; j < N; ++j) {
             float w = 0.0f;
@@ -1000,7 +1013,7 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
             if (all_views)
                 CA(s, j) = c;
             else if (geom)
-                acc += w * (c + 0.1f * geom_cost(V, j, pl, px, py));
+                acc += w * (c + 0.1f * geom_cost(V, j, gp, px, py));
             else
                 acc += w * c;
         }
