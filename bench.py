@@ -42,6 +42,9 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-view comparison step")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-serving", action="store_true", help="skip the served-stream latency measurement")
+    ap.add_argument("--batching", action="store_true",
+                    help="measure the batching form instead: reference views of uneven size and source count "
+                         "from four scenes, one launch per stage against one launch chain per view")
     ap.add_argument("--split", action="store_true",
                     help="with --profile: run every half-sweep as two kernels (neighbours, then the rest)")
     ap.add_argument("--ref-views", type=int, default=0,
@@ -224,11 +227,78 @@ def segments_run(dev) -> dict:
     return out
 
 
+BATCH_SIZES = ((480, 640), (960, 1280), (1200, 1600), (1800, 2400), (2400, 3200))
+
+
+def batching_run(dev, n_views: int = 16, seed: int = 0, sizes=BATCH_SIZES) -> dict:
+    """Batching form: n_views reference views drawn from four room scenes
+    (seeds 0-3), each scene at a resolution drawn from `sizes` (H, W), 4-12
+    sources per view; the random pass (init + 3 iterations) as one launch
+    per stage over all of them, and as one launch chain per view,
+    CUDA-event timed on one stream."""
+    import numpy as np
+    import torch
+
+    from gmvs_gb300 import _abi, engine, synthetic
+
+    rng = np.random.default_rng(seed)
+    views, mix = [], []
+    per_scene = n_views // 4
+    for sd in range(4):
+        H, W = sizes[int(rng.integers(len(sizes)))]
+        sc = synthetic.room_scene(sd, H=H, W=W, num_views=16, num_src=12, device=dev)
+        imgs = torch.from_numpy(sc.images.astype(np.float32)).to(dev)
+        cams = [engine.make_camera(*synthetic.camera_args(sc, i)) for i in range(sc.num_views)]
+        for ref, src in sc.problems[:per_scene]:
+            n = int(rng.integers(4, 13))
+            ids = [ref] + list(src)[:n]
+            v = engine.ViewInputs(cams=[cams[i] for i in ids], images=[imgs[i] for i in ids],
+                                  depth_min=sc.depth_range[0] * 0.6, depth_max=sc.depth_range[1] * 1.2,
+                                  stream_id=ref)
+            v.allocate_outputs()
+            views.append(v)
+            mix.append(f"{W}x{H}/{len(ids) - 1}")
+    p = engine.params_struct(sampler=_abi.SAMPLER_TEX)
+    ws = engine.Workspace(dev)
+    batched = engine.Plan(views, p, ws)
+    singles = [engine.Plan([v], p, engine.Workspace(dev)) for v in views]
+    st = torch.cuda.current_stream()
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    ms_batched = timed(lambda: batched.launch(st))
+    batched_depth = [v.out_depth.clone() for v in views]
+    ms_single = timed(lambda: [pl.launch(st) for pl in singles])
+    # the batched launch and the per-view chains compute one thing
+    same = all(torch.equal(a, v.out_depth) for a, v in zip(batched_depth, views))
+    px = sum(v.height * v.width for v in views)
+    for pl in singles + [batched]:
+        pl.close()
+    return {"views": len(views), "megapixels": round(px / 1e6, 2), "mix": mix,
+            "random_pass_ms_one_launch_per_stage": ms_batched, "random_pass_ms_one_chain_per_view": ms_single,
+            "speedup": ms_single / ms_batched, "outputs_equal": same}
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
     import numpy as np
     import torch
+
+    if args.batching:
+        if rank == 0:
+            dev = torch.device("cuda", local)
+            print(json.dumps({"batching_form": {"all_sizes": batching_run(dev),
+                                                "small_sizes": batching_run(dev, sizes=BATCH_SIZES[:2])}}))
+        return
 
     if args.impl == "reference":
         if rank != 0:
