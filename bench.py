@@ -227,6 +227,38 @@ def segments_run(dev) -> dict:
     return out
 
 
+def superpixels_run(dev, n_images: int = 8, workers: int = 4) -> dict:
+    """The segmentation preprocessing (extract_superpixel.py seg_func's
+    segment-id map) on 1600x1200 BGR images from host memory: one image at a
+    time and `workers` at a time (wall clock, host copies included), beside
+    the oracle's CPU restatement of one image (numpy + a Python merge)."""
+    import torch
+
+    import oracle.superpixel as osp
+    from gmvs_gb300 import superpixel as sp
+    from gmvs_gb300.synthetic import indoor_image
+
+    imgs = [indoor_image(1200, 1600, s) for s in range(n_images)]
+    for b, g in imgs[:2]:
+        sp.segment_ids(b, g)
+    sp.extract_many([b for b, _ in imgs[:workers]], [g for _, g in imgs[:workers]], workers=workers)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for b, g in imgs:
+        sp.segment_ids(b, g)
+    one_ms = (time.perf_counter() - t0) / n_images * 1000.0
+    t0 = time.perf_counter()
+    sp.extract_many([b for b, _ in imgs], [g for _, g in imgs], workers=workers)
+    many_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    osp.segment_ids(imgs[0][0], imgs[0][1])
+    cpu_s = time.perf_counter() - t0
+    return {"size": "1600x1200", "working_size": "384x288", "images": n_images,
+            "ms_per_image_one_at_a_time": one_ms, "images_per_s": n_images / many_s, "workers": workers,
+            "cpu_baseline": {"s_per_image": cpu_s, "kind": "port", "cores": 1,
+                             "sample": "oracle segment-id map of one 1600x1200 image"}}
+
+
 BATCH_SIZES = ((480, 640), (960, 1280), (1200, 1600), (1800, 2400), (2400, 3200))
 
 
@@ -424,6 +456,7 @@ def main():
     if not args.no_serving and rank == 0:
         served = serving_run(dev)
     segments = segments_run(dev) if rank == 0 else None
+    superpixels = superpixels_run(dev) if rank == 0 else None
 
     if rank != 0:
         return
@@ -465,6 +498,7 @@ def main():
                      "note": "batched: every view of the scene completes with the step"}),
         "serving": served,
         "segments": segments,
+        "superpixels": superpixels,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
                      "kernel": "k_sweep (half-sweep over all views)", "peak_source": peak_note,

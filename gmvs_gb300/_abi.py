@@ -64,6 +64,11 @@ class gmvs_fuse_view(ctypes.Structure):
                 ("out_normal", _p), ("out_count", _p)]
 
 
+class gmvs_superpixel_params(ctypes.Structure):
+    _fields_ = [("seg_rows", _i), ("seg_cols", _i), ("scale", ctypes.c_double), ("sigma", ctypes.c_double),
+                ("min_size", _i), ("close_size", _i), ("var_windlen", _i), ("var_thresh", _f)]
+
+
 _SIGS = {
     "gmvs_version": (_i, []),
     "gmvs_last_error": (ctypes.c_char_p, []),
@@ -98,6 +103,11 @@ _SIGS = {
     "gmvs_gather_workspace_bytes": (ctypes.c_size_t, [_i, _i]),
     "gmvs_gather_points": (_i, [_p, _p, _i, _i, _p, _p, _f, _p, _p, _p, _p, _p, _p, ctypes.c_size_t, _p]),
     "gmvs_view_scores": (_i, [_p, _p, _i, _p, _i, _p, _p, _p]),
+    "gmvs_superpixel_default_params": (None, [ctypes.POINTER(gmvs_superpixel_params)]),
+    "gmvs_superpixel_workspace_bytes": (ctypes.c_size_t, [_i, _i, ctypes.POINTER(gmvs_superpixel_params)]),
+    "gmvs_superpixel_labels_host": (_i, [_i, _i, _p, ctypes.c_double, _i, _p, _p]),
+    "gmvs_superpixels": (_i, [_p, _p, _p, _i, _i, ctypes.POINTER(gmvs_superpixel_params), _p, _p, _p, _p, _p, _p,
+                              ctypes.c_size_t, _p]),
 }
 
 EXPORTED = tuple(_SIGS)

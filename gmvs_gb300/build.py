@@ -41,7 +41,9 @@ SOURCES = {
     "segments.cu": [],
     "gather.cu": [],
     "views.cu": [],
+    "superpixel.cu": [],
     "prior.cpp": [],
+    "felzenszwalb.cpp": [],
 }
 
 

@@ -359,3 +359,30 @@ def superpixel_case(rows: int, cols: int, seed: int, cell=(24, 20)):
     n = (n / np.linalg.norm(n, axis=-1, keepdims=True)).astype(np.float32)
     var = rng.random((rows, cols)).astype(np.float32) * np.where(kind % 2 == 0, 0.4, 1.0)[seg].astype(np.float32)
     return seg, planar, n, var
+
+
+def indoor_image(rows: int, cols: int, seed: int = 0, textured: int = 3):
+    """A BGR uint8 [rows, cols, 3] picture of flat-coloured walls and boxes
+    with mild shading and sensor noise plus `textured` patches of strong
+    texture, and its gray uint8 image: segments with low and with high local
+    variance for the superpixel extraction.  Returns (bgr, gray)."""
+    rng = np.random.default_rng(seed)
+    ys, xs = np.mgrid[0:rows, 0:cols].astype(np.float64)
+    img = np.empty((rows, cols, 3))
+    base = rng.uniform(60, 200, 3)
+    img[:] = base + 20.0 * (ys / rows)[..., None]
+    horizon = int(rows * rng.uniform(0.55, 0.75))
+    img[horizon:] = rng.uniform(40, 160, 3) + 15.0 * (xs[horizon:] / cols)[..., None]
+    for _ in range(int(rng.integers(6, 12))):
+        h, w = int(rng.integers(rows // 10, rows // 3)), int(rng.integers(cols // 10, cols // 3))
+        y0, x0 = int(rng.integers(0, rows - h)), int(rng.integers(0, cols - w))
+        img[y0:y0 + h, x0:x0 + w] = rng.uniform(20, 235, 3)
+    for _ in range(textured):
+        h, w = int(rng.integers(rows // 12, rows // 5)), int(rng.integers(cols // 12, cols // 5))
+        y0, x0 = int(rng.integers(0, rows - h)), int(rng.integers(0, cols - w))
+        img[y0:y0 + h, x0:x0 + w] += rng.normal(0, 45, (h, w, 3))
+    img += rng.normal(0, 1.5, img.shape)
+    bgr = np.clip(np.rint(img), 0, 255).astype(np.uint8)
+    x = bgr.astype(np.float64)
+    gray = np.clip(np.rint(0.114 * x[..., 0] + 0.587 * x[..., 1] + 0.299 * x[..., 2]), 0, 255).astype(np.uint8)
+    return bgr, gray

@@ -333,6 +333,53 @@ GMVS_API int32_t gmvs_view_scores(const long long* offsets, const int32_t* point
                          const double* xyz, int32_t num_points, const double* centers, float* scores,
                          void* stream);
 
+/* -------------------------------------------------------------- superpixels --
+ * The segmentation preprocessing of gmvs/scripts/extract_superpixel.py:
+ * extract_superpixel (lines 55-74: resize to seg_cols x seg_rows,
+ * Felzenszwalb segmentation, segments of at most seg_rows * seg_cols / 128
+ * pixels dropped, nearest resize back) and seg_func's segment-id map
+ * (lines 77-113: a close_size x close_size morphological close, an
+ * optional mask with its small-segment filter, and the variance filter
+ * where(winVar(gray / 255, var_windlen) / max < var_thresh, ids, 0)).
+ * No counterpart in the reference's C++ (it is a Python script over OpenCV
+ * and scikit-image). */
+typedef struct gmvs_superpixel_params {
+    int32_t seg_rows;    /* working size of the segmentation (288) */
+    int32_t seg_cols;    /* (384) */
+    double scale;        /* Felzenszwalb scale (100) */
+    double sigma;        /* Gaussian pre-smoothing (0.5; <= 0: none) */
+    int32_t min_size;    /* minimum component size of the second merge pass (5) */
+    int32_t close_size;  /* odd box of the morphological close (11) */
+    int32_t var_windlen; /* box of the variance map (15); <= 1 turns the variance filter off */
+    float var_thresh;    /* (0.2); <= 0 turns the variance filter off */
+} gmvs_superpixel_params;
+
+GMVS_API void gmvs_superpixel_default_params(gmvs_superpixel_params* out);
+GMVS_API size_t gmvs_superpixel_workspace_bytes(int32_t rows, int32_t cols, const gmvs_superpixel_params* params);
+/* image: device uint8 [rows][cols][3] (channel order as read, BGR from
+ * OpenCV); gray: device uint8 [rows][cols], needed when the variance filter
+ * is on and out_ids_map or out_var_map is given; mask: device uint8
+ * [rows][cols], nonzero = keep, or NULL.  Outputs (device, each optional):
+ * out_segment int32 [rows][cols] = extract_superpixel's labels;
+ * out_ids uint8 = segment ids after the close (and mask);
+ * out_ids_map int32 = the variance-filtered ids (the ids themselves when
+ * the filter is off); out_var_map float = the normalised variance map.
+ * out_num_segments (host, optional) = segments kept by the size filter.
+ * The Felzenszwalb merge runs on the calling thread between the device
+ * stages, so the call synchronises `stream` once and returns with the
+ * remaining kernels queued on it. */
+/* The host half alone, on host arrays: weights of the right, down,
+ * down-right and up-right edges of a rows x cols grid, each group in raster
+ * order ((rows * (cols - 1) + (rows - 1) * cols + 2 (rows - 1)(cols - 1))
+ * non-negative values); writes labels [rows][cols] after the merge and the
+ * size filter (0 = dropped or the first segment). */
+GMVS_API int32_t gmvs_superpixel_labels_host(int32_t rows, int32_t cols, const double* weights, double scale,
+                                    int32_t min_size, int32_t* labels, int32_t* out_num_segments);
+GMVS_API int32_t gmvs_superpixels(const uint8_t* image, const uint8_t* gray, const uint8_t* mask, int32_t rows,
+                         int32_t cols, const gmvs_superpixel_params* params, int32_t* out_segment,
+                         uint8_t* out_ids, int32_t* out_ids_map, float* out_var_map,
+                         int32_t* out_num_segments, void* workspace, size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
