@@ -23,9 +23,12 @@ struct SampF32 {  // plain fp32 rows, four loads per sample
     static constexpr bool kTex = false;
 };
 
-// Texel quads: quad[y][x] = (I[y][x], I[y][xu], I[yu][x], I[yu][xu]) with
-// xu = min(x+1, W-1), yu = min(y+1, H-1), i.e. the four taps the reference
-// reads for a sample whose clamped integer corner is (x, y).
+// Texel quads: quad[y][x] = (a, b - a, c, d - c) for the four taps the
+// reference reads for a sample whose clamped integer corner is (x, y):
+// a = I[y][x], b = I[y][xu], c = I[yu][x], d = I[yu][xu] with
+// xu = min(x+1, W-1), yu = min(y+1, H-1).  The differences are the ones the
+// interpolation fma(w, b - a, a) forms, rounded the same way at staging, so
+// the sample is unchanged and costs two subtractions less.
 // hl = clamp(trunc(v), 0, H - 1) exactly as the reference, without int/float
 // conversions: clamping first makes trunc == floor, and adding 2^23 with
 // round-down leaves floor(v) in the low mantissa bits.  NaN -> 0 and +-inf
@@ -53,7 +56,7 @@ struct SampQuadF32 {
         float wd, hd;
         clamp_corner(u, v, H, W, idx, wd, hd);
         const float4 q = __ldg(&p[GMVS_IDX(idx, H * W, kOobImage)]);
-        return lerpf(lerpf(q.x, q.y, wd), lerpf(q.z, q.w, wd), hd);
+        return lerpf(fmaf(wd, q.y, q.x), fmaf(wd, q.w, q.z), hd);
     }
     static constexpr bool kTex = false;
 };
@@ -76,7 +79,7 @@ struct SampQuadF16 {
         clamp_corner(u, v, H, W, idx, wd, hd);
         const uint2 q = __ldg(&p[GMVS_IDX(idx, H * W, kOobImage)]);
         const float2 t = h2f(q.x), b = h2f(q.y);
-        return lerpf(lerpf(t.x, t.y, wd), lerpf(b.x, b.y, wd), hd);
+        return lerpf(fmaf(wd, t.y, t.x), fmaf(wd, b.y, b.x), hd);
     }
     static constexpr bool kTex = false;
 };

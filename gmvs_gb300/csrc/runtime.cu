@@ -96,23 +96,29 @@ __global__ void k_filter(const DevView* __restrict__ views, const Tile* __restri
     }
 }
 
-// texel quads for the CLAMP sampler (see SampQuadF32)
+// texel quads for the CLAMP sampler (see SampQuadF32): (a, b - a, c, d - c)
+// for the texels a b / c d at (x, y), (x+1, y), (x, y+1), (x+1, y+1), the
+// differences rounded to fp32 as the sampler's interpolation forms them
 __global__ void k_stage_quad_f32(const float* __restrict__ img, float4* __restrict__ out, int H, int W) {
     const int n = H * W;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int y = i / W, x = i - y * W;
         const int xu = min(x + 1, W - 1), yu = min(y + 1, H - 1);
-        out[i] = make_float4(img[y * W + x], img[y * W + xu], img[yu * W + x], img[yu * W + xu]);
+        const float a = img[y * W + x], b = img[y * W + xu], c = img[yu * W + x], d = img[yu * W + xu];
+        out[i] = make_float4(a, b - a, c, d - c);
     }
 }
+// fp16 quads are staged only for integer images in [0, 2048], whose values
+// and differences are exact in fp16
 __global__ void k_stage_quad_f16(const float* __restrict__ img, uint2* __restrict__ out, int H, int W) {
     const int n = H * W;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int y = i / W, x = i - y * W;
         const int xu = min(x + 1, W - 1), yu = min(y + 1, H - 1);
-        __half2 t = __floats2half2_rn(img[y * W + x], img[y * W + xu]);
-        __half2 b = __floats2half2_rn(img[yu * W + x], img[yu * W + xu]);
-        out[i] = make_uint2(*reinterpret_cast<uint32_t*>(&t), *reinterpret_cast<uint32_t*>(&b));
+        const float a = img[y * W + x], b = img[y * W + xu], c = img[yu * W + x], d = img[yu * W + xu];
+        __half2 t = __floats2half2_rn(a, b - a);
+        __half2 u = __floats2half2_rn(c, d - c);
+        out[i] = make_uint2(*reinterpret_cast<uint32_t*>(&t), *reinterpret_cast<uint32_t*>(&u));
     }
 }
 // 1 when every pixel is an integer in [0, 2048] (exact in fp16), else 0
