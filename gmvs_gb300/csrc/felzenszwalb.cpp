@@ -29,30 +29,22 @@ int32_t fail(int32_t code, const std::string& msg);
 
 namespace {
 
-void edge_ends(int rows, int cols, int64_t e, int32_t& a, int32_t& b) {
-    const int64_t nr = (int64_t)rows * (cols - 1), nd = (int64_t)(rows - 1) * cols,
-                  ng = (int64_t)(rows - 1) * (cols - 1);
-    if (e < nr) {
-        const int64_t y = e / (cols - 1), x = e % (cols - 1), p = y * cols + x;
-        a = (int32_t)p, b = (int32_t)(p + 1);
-        return;
-    }
-    e -= nr;
-    if (e < nd) {
-        a = (int32_t)e, b = (int32_t)(e + cols);
-        return;
-    }
-    e -= nd;
-    const bool up = e >= ng;
-    if (up) e -= ng;
-    const int64_t y = e / (cols - 1), x = e % (cols - 1), p = y * cols + x;
-    if (!up)
-        a = (int32_t)p, b = (int32_t)(p + cols + 1);
-    else
-        a = (int32_t)(p + 1), b = (int32_t)(p + cols);
+// endpoints of every edge, in edge order (no divisions in the merge loops)
+void edge_ends(int rows, int cols, std::vector<int32_t>& ea, std::vector<int32_t>& eb) {
+    int64_t e = 0;
+    for (int y = 0; y < rows; ++y)  // right
+        for (int x = 0; x + 1 < cols; ++x, ++e) ea[e] = y * cols + x, eb[e] = y * cols + x + 1;
+    for (int y = 0; y + 1 < rows; ++y)  // down
+        for (int x = 0; x < cols; ++x, ++e) ea[e] = y * cols + x, eb[e] = (y + 1) * cols + x;
+    for (int y = 0; y + 1 < rows; ++y)  // down-right
+        for (int x = 0; x + 1 < cols; ++x, ++e) ea[e] = y * cols + x, eb[e] = (y + 1) * cols + x + 1;
+    for (int y = 0; y + 1 < rows; ++y)  // up-right
+        for (int x = 0; x + 1 < cols; ++x, ++e) ea[e] = y * cols + x + 1, eb[e] = (y + 1) * cols + x;
 }
 
-// stable ascending order of non-negative doubles: 4 passes of 16-bit digits
+// stable ascending order of non-negative doubles: LSD radix sort with 8-bit
+// digits (256 buckets keep the scatter cache-friendly); a pass whose digit
+// is the same for every key is skipped
 std::vector<uint32_t> sort_edges(const double* w, int64_t n) {
     std::vector<uint64_t> key(n), key2(n);
     std::vector<uint32_t> idx(n), idx2(n);
@@ -60,19 +52,20 @@ std::vector<uint32_t> sort_edges(const double* w, int64_t n) {
         std::memcpy(&key[i], &w[i], 8);
         idx[i] = (uint32_t)i;
     }
-    std::vector<int64_t> count(65537);
-    for (int pass = 0; pass < 4; ++pass) {
-        const int sh = 16 * pass;
-        std::fill(count.begin(), count.end(), 0);
-        for (int64_t i = 0; i < n; ++i) ++count[((key[i] >> sh) & 0xffff) + 1];
+    int64_t count[8][257] = {};
+    for (int64_t i = 0; i < n; ++i)
+        for (int d = 0; d < 8; ++d) ++count[d][((key[i] >> (8 * d)) & 0xff) + 1];
+    for (int d = 0; d < 8; ++d) {
+        int64_t* c = count[d];
         bool trivial = false;
-        for (int d = 1; d <= 65536; ++d) {
-            if (count[d] == n) trivial = true;
-            count[d] += count[d - 1];
+        for (int k = 1; k <= 256; ++k) {
+            if (c[k] == n) trivial = true;
+            c[k] += c[k - 1];
         }
         if (trivial) continue;  // every key has the same digit: the order stands
+        const int sh = 8 * d;
         for (int64_t i = 0; i < n; ++i) {
-            const int64_t at = count[(key[i] >> sh) & 0xffff]++;
+            const int64_t at = c[(key[i] >> sh) & 0xff]++;
             key2[at] = key[i];
             idx2[at] = idx[i];
         }
@@ -82,27 +75,33 @@ std::vector<uint32_t> sort_edges(const double* w, int64_t n) {
     return idx;
 }
 
+// one 16-byte node per pixel: a find and the size / inner-cost test that
+// follows touch one cache line
+struct Node {
+    int32_t parent, size;
+    double inner;
+};
+
 struct Forest {
-    std::vector<int32_t> parent, size;
-    std::vector<double> inner;
-    explicit Forest(int32_t n) : parent(n), size(n, 1), inner(n, 0.0) {
-        for (int32_t i = 0; i < n; ++i) parent[i] = i;
+    std::vector<Node> node;
+    explicit Forest(int32_t n) : node(n) {
+        for (int32_t i = 0; i < n; ++i) node[i] = Node{i, 1, 0.0};
     }
     int32_t find(int32_t a) {
         int32_t r = a;
-        while (parent[r] != r) r = parent[r];
-        while (parent[a] != r) {
-            const int32_t nx = parent[a];
-            parent[a] = r;
+        while (node[r].parent != r) r = node[r].parent;
+        while (node[a].parent != r) {
+            const int32_t nx = node[a].parent;
+            node[a].parent = r;
             a = nx;
         }
         return r;
     }
     int32_t join(int32_t a, int32_t b) {
         const int32_t r = std::min(a, b);
-        const int32_t s = size[a] + size[b];
-        parent[a] = parent[b] = r;
-        size[r] = s;
+        const int32_t s = node[a].size + node[b].size;
+        node[a].parent = node[b].parent = r;
+        node[r].size = s;
         return r;
     }
 };
@@ -113,23 +112,26 @@ int32_t superpixel_labels(int rows, int cols, const double* weights, double k, i
     const int32_t n = rows * cols;
     const int64_t ne = (int64_t)rows * (cols - 1) + (int64_t)(rows - 1) * cols + 2LL * (rows - 1) * (cols - 1);
     const std::vector<uint32_t> order = sort_edges(weights, ne);
+    // endpoints and weights in visiting order: both passes stream them
+    std::vector<int32_t> ea(ne), eb(ne), sa(ne), sb(ne);
+    std::vector<double> sw(ne);
+    edge_ends(rows, cols, ea, eb);
+    for (int64_t i = 0; i < ne; ++i) {
+        const uint32_t e = order[i];
+        sa[i] = ea[e], sb[i] = eb[e], sw[i] = weights[e];
+    }
     Forest f(n);
     for (int64_t i = 0; i < ne; ++i) {
-        int32_t a, b;
-        edge_ends(rows, cols, order[i], a, b);
-        a = f.find(a), b = f.find(b);
+        const int32_t a = f.find(sa[i]), b = f.find(sb[i]);
         if (a == b) continue;
-        const double w = weights[order[i]];
-        const double ta = f.inner[a] + k / (double)f.size[a];
-        const double tb = f.inner[b] + k / (double)f.size[b];
-        if (w < std::min(ta, tb)) f.inner[f.join(a, b)] = w;
+        const double ta = f.node[a].inner + k / (double)f.node[a].size;
+        const double tb = f.node[b].inner + k / (double)f.node[b].size;
+        if (sw[i] < std::min(ta, tb)) f.node[f.join(a, b)].inner = sw[i];
     }
     for (int64_t i = 0; i < ne; ++i) {
-        int32_t a, b;
-        edge_ends(rows, cols, order[i], a, b);
-        a = f.find(a), b = f.find(b);
+        const int32_t a = f.find(sa[i]), b = f.find(sb[i]);
         if (a == b) continue;
-        if (f.size[a] < min_size || f.size[b] < min_size) f.join(a, b);
+        if (f.node[a].size < min_size || f.node[b].size < min_size) f.join(a, b);
     }
     // labels by root order, then the size filter: label 0 stays 0, every
     // other label with more than rows * cols / 128 pixels is renumbered

@@ -5,12 +5,13 @@
 // (felzenszwalb.cpp) between the two device halves:
 //
 //   image [rows][cols][3] u8 --k_resize--> small [seg_rows][seg_cols][3] u8
-//     --k_gauss_rows, k_gauss_cols--> smoothed FP64 (x / 255 scaled first)
+//     --k_gauss_rows, k_gauss_cols--> smoothed FP64 (of x * (1 / 255))
 //     --k_edge_weights--> 4 edge groups of FP64 weights --D2H-->
 //   host: stable sort, two merge passes, labels, size filter --H2D-->
-//     labels [seg_rows][seg_cols] --k_up_dilate_rows (nearest resize fused
-//     with the row maximum), k_dilate_cols, k_erode_rows,
-//     k_erode_cols_ids--> closed ids u8 [rows][cols] (mask and its
+//     labels [seg_rows][seg_cols] --k_nearest_tables, k_up_dilate_rows
+//     (nearest resize fused with the row maximum), k_box_extreme (column
+//     maximum, row minimum), k_erode_cols_ids (column minimum)--> closed
+//     ids u8 [rows][cols] (mask and its
 //     per-id histogram fused), k_mask_filter
 //   gray u8 --k_box_rows, k_box_cols_var--> sqrt|E[g^2] - E[g]^2| and its
 //     maximum --k_var_apply--> var map f32, where(var < thresh, ids, 0).
@@ -50,7 +51,7 @@ __host__ __device__ inline int reflect_index(int i, int n) {
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct SpLayout {
-    size_t small, gtmp, smooth, weights, labels, a, b, ids, s1, s2, var, vmax, hist, total;
+    size_t small, gtmp, smooth, weights, labels, sxs, sys, a, b, ids, s1, s2, var, vmax, hist, total;
     int64_t ne;
 };
 
@@ -70,6 +71,8 @@ SpLayout sp_layout(int rows, int cols, const gmvs_superpixel_params& p) {
     L.smooth = take(ns * 3 * sizeof(double));
     L.weights = take((size_t)std::max<int64_t>(L.ne, 1) * sizeof(double));
     L.labels = take(ns * sizeof(int32_t));
+    L.sxs = take((size_t)cols * sizeof(int32_t));
+    L.sys = take((size_t)rows * sizeof(int32_t));
     L.a = take(n * sizeof(int32_t));
     L.b = take(n * sizeof(int32_t));
     L.ids = take(n);
@@ -196,26 +199,29 @@ __global__ void k_edge_weights(const double* __restrict__ sm, int h, int w, doub
 
 // -------------------------------------------------- nearest resize + close --
 // Nearest resize back to full size (OpenCV INTER_NEAREST:
-// src = min(floor(dst * (1 / (dst_size / src_size))), src_size - 1)) fused
-// with the first pass of the close: a box maximum along the row over the
-// pixels inside the image (the close's dilation, then erosion, with a
-// close_size box; the border takes no part).
-__global__ void k_up_dilate_rows(const int32_t* __restrict__ lbl, int sh, int sw, int H, int W, double ifx,
-                                 double ify, int lo, int hi, int32_t* __restrict__ seg_out,
-                                 int32_t* __restrict__ out) {
+// src = min(floor(dst * (1 / (dst_size / src_size))), src_size - 1)), one
+// table entry per full-size column and row.
+__global__ void k_nearest_tables(int W, int H, int sw, int sh, double ifx, double ify, int32_t* __restrict__ sxs,
+                                 int32_t* __restrict__ sys) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < W) sxs[i] = min((int)floor((double)i * ifx), sw - 1);
+    if (i < H) sys[i] = min((int)floor((double)i * ify), sh - 1);
+}
+
+// The resize fused with the first pass of the close: a box maximum along the
+// row over the pixels inside the image (the close's dilation, then erosion,
+// with a close_size box; the border takes no part).
+__global__ void k_up_dilate_rows(const int32_t* __restrict__ lbl, int sw, int H, int W,
+                                 const int32_t* __restrict__ sxs, const int32_t* __restrict__ sys, int lo, int hi,
+                                 int32_t* __restrict__ seg_out, int32_t* __restrict__ out) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= W || y >= H) return;
-    const int sy = min((int)floor((double)y * ify), sh - 1);
-    const int32_t* row = lbl + (size_t)sy * sw;
+    const int32_t* row = lbl + (size_t)sys[y] * sw;
     int m = INT_MIN;
-    for (int k = lo; k <= hi; ++k) {
-        const int xx = x + k;
-        if (xx < 0 || xx >= W) continue;
-        m = max(m, row[min((int)floor((double)xx * ifx), sw - 1)]);
-    }
+    for (int k = max(lo, -x); k <= min(hi, W - 1 - x); ++k) m = max(m, row[sxs[x + k]]);
     const size_t p = (size_t)y * W + x;
     out[p] = m;
-    if (seg_out) seg_out[p] = row[min((int)floor((double)x * ifx), sw - 1)];
+    if (seg_out) seg_out[p] = row[sxs[x]];
 }
 
 template <bool kMax, bool kAlongRow>
@@ -291,12 +297,16 @@ __global__ void k_mask_filter(uint8_t* __restrict__ ids, size_t n, const int32_t
 // sqrt(|E[g^2] - E[g]^2|) and its maximum.
 __global__ void k_box_rows(const uint8_t* __restrict__ gray, int H, int W, int lo, int hi, double* __restrict__ s1,
                            double* __restrict__ s2) {
+    __shared__ double level[256];  // g / 255 for every gray level: one FP64 division each
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    for (int i = t; i < 256; i += blockDim.x * blockDim.y) level[i] = (double)i / 255.0;
+    __syncthreads();
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= W || y >= H) return;
     const uint8_t* row = gray + (size_t)y * W;
     double a = 0.0, b = 0.0;
     for (int k = lo; k <= hi; ++k) {
-        const double v = (double)row[reflect_index(x + k, W)] / 255.0;
+        const double v = level[row[reflect_index(x + k, W)]];
         a = a + v;
         b = b + v * v;
     }
@@ -447,12 +457,18 @@ extern "C" int32_t gmvs_superpixels(const uint8_t* image, const uint8_t* gray, c
     const dim3 g2((cols + 31) / 32, (rows + 7) / 8);
     const double ifx = 1.0 / ((double)cols / sw), ify = 1.0 / ((double)rows / sh);
     const bool need_ids = out_ids || out_ids_map;
+    int32_t* sxs = (int32_t*)(ws + L.sxs);
+    int32_t* sys = (int32_t*)(ws + L.sys);
+    if (need_ids || out_segment) {
+        const int m = std::max(rows, cols);
+        k_nearest_tables<<<(m + 255) / 256, 256, 0, st>>>(cols, rows, sw, sh, ifx, ify, sxs, sys);
+    }
     int32_t* a = (int32_t*)(ws + L.a);
     int32_t* b = (int32_t*)(ws + L.b);
     uint8_t* ids = out_ids ? out_ids : (uint8_t*)(ws + L.ids);
     const int lo = -(P.close_size / 2), hi = P.close_size - 1 - P.close_size / 2;
     if (need_ids) {
-        k_up_dilate_rows<<<g2, b2, 0, st>>>((const int32_t*)(ws + L.labels), sh, sw, rows, cols, ifx, ify, lo, hi,
+        k_up_dilate_rows<<<g2, b2, 0, st>>>((const int32_t*)(ws + L.labels), sw, rows, cols, sxs, sys, lo, hi,
                                             out_segment, a);
         k_box_extreme<true, false><<<g2, b2, 0, st>>>(a, rows, cols, lo, hi, b);
         k_box_extreme<false, true><<<g2, b2, 0, st>>>(b, rows, cols, lo, hi, a);
@@ -467,7 +483,7 @@ extern "C" int32_t gmvs_superpixels(const uint8_t* image, const uint8_t* gray, c
             k_mask_filter<<<grid_1d(n), 256, 0, st>>>(ids, n, hist);
         }
     } else if (out_segment) {
-        k_up_dilate_rows<<<g2, b2, 0, st>>>((const int32_t*)(ws + L.labels), sh, sw, rows, cols, ifx, ify, 0, 0,
+        k_up_dilate_rows<<<g2, b2, 0, st>>>((const int32_t*)(ws + L.labels), sw, rows, cols, sxs, sys, 0, 0,
                                             out_segment, a);
     }
     if (var_on && (out_ids_map || out_var_map)) {
