@@ -108,18 +108,9 @@ struct Forest {
 
 }  // namespace
 
-int32_t superpixel_labels(int rows, int cols, const double* weights, double k, int min_size, int32_t* labels) {
+int32_t superpixel_merge_sorted(int rows, int cols, int64_t ne, const int32_t* sa, const int32_t* sb,
+                                const double* sw, double k, int min_size, int32_t* labels) {
     const int32_t n = rows * cols;
-    const int64_t ne = (int64_t)rows * (cols - 1) + (int64_t)(rows - 1) * cols + 2LL * (rows - 1) * (cols - 1);
-    const std::vector<uint32_t> order = sort_edges(weights, ne);
-    // endpoints and weights in visiting order: both passes stream them
-    std::vector<int32_t> ea(ne), eb(ne), sa(ne), sb(ne);
-    std::vector<double> sw(ne);
-    edge_ends(rows, cols, ea, eb);
-    for (int64_t i = 0; i < ne; ++i) {
-        const uint32_t e = order[i];
-        sa[i] = ea[e], sb[i] = eb[e], sw[i] = weights[e];
-    }
     Forest f(n);
     for (int64_t i = 0; i < ne; ++i) {
         const int32_t a = f.find(sa[i]), b = f.find(sb[i]);
@@ -151,6 +142,20 @@ int32_t superpixel_labels(int rows, int cols, const double* weights, double k, i
         if (count[l] * 128 > (int64_t)n) keep[l] = ++kept;
     for (int32_t i = 0; i < n; ++i) labels[i] = keep[labels[i]];
     return kept;
+}
+
+int32_t superpixel_labels(int rows, int cols, const double* weights, double k, int min_size, int32_t* labels) {
+    const int64_t ne = (int64_t)rows * (cols - 1) + (int64_t)(rows - 1) * cols + 2LL * (rows - 1) * (cols - 1);
+    const std::vector<uint32_t> order = sort_edges(weights, ne);
+    // endpoints and weights in visiting order: both passes stream them
+    std::vector<int32_t> ea(ne), eb(ne), sa(ne), sb(ne);
+    std::vector<double> sw(ne);
+    edge_ends(rows, cols, ea, eb);
+    for (int64_t i = 0; i < ne; ++i) {
+        const uint32_t e = order[i];
+        sa[i] = ea[e], sb[i] = eb[e], sw[i] = weights[e];
+    }
+    return superpixel_merge_sorted(rows, cols, ne, sa.data(), sb.data(), sw.data(), k, min_size, labels);
 }
 
 }  // namespace gmvs

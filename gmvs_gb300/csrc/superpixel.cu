@@ -6,8 +6,9 @@
 //
 //   image [rows][cols][3] u8 --k_resize--> small [seg_rows][seg_cols][3] u8
 //     --k_gauss_rows, k_gauss_cols--> smoothed FP64 (of x * (1 / 255))
-//     --k_edge_weights--> 4 edge groups of FP64 weights --D2H-->
-//   host: stable sort, two merge passes, labels, size filter --H2D-->
+//     --k_edge_weights--> 4 edge groups of FP64 weights --k_sort_* (stable
+//     radix sort), k_sorted_ends--> edges in visiting order --D2H-->
+//   host: two merge passes, labels, size filter --H2D-->
 //     labels [seg_rows][seg_cols] --k_nearest_tables, k_up_dilate_rows
 //     (nearest resize fused with the row maximum), k_box_extreme (column
 //     maximum, row minimum), k_erode_cols_ids (column minimum)--> closed
@@ -50,9 +51,13 @@ __host__ __device__ inline int reflect_index(int i, int n) {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+constexpr int kSortChunk = 2048;  // edges per block and radix pass (8 tiles of 256)
+
 struct SpLayout {
-    size_t small, gtmp, smooth, weights, labels, sxs, sys, a, b, ids, s1, s2, var, vmax, hist, total;
+    size_t small, gtmp, smooth, weights, keys2, vals, vals2, counts, ends_a, ends_b, sort_err, labels, sxs, sys, a, b,
+        ids, s1, s2, var, vmax, hist, total;
     int64_t ne;
+    int sort_blocks;
 };
 
 SpLayout sp_layout(int rows, int cols, const gmvs_superpixel_params& p) {
@@ -69,7 +74,16 @@ SpLayout sp_layout(int rows, int cols, const gmvs_superpixel_params& p) {
     L.small = take(ns * 3);
     L.gtmp = take(ns * 3 * sizeof(double));
     L.smooth = take(ns * 3 * sizeof(double));
-    L.weights = take((size_t)std::max<int64_t>(L.ne, 1) * sizeof(double));
+    const size_t ne1 = (size_t)std::max<int64_t>(L.ne, 1);
+    L.sort_blocks = (int)((ne1 + kSortChunk - 1) / kSortChunk);
+    L.weights = take(ne1 * sizeof(double));  // sorted in place: the weights in visiting order
+    L.keys2 = take(ne1 * sizeof(double));
+    L.vals = take(ne1 * sizeof(uint32_t));
+    L.vals2 = take(ne1 * sizeof(uint32_t));
+    L.counts = take((size_t)256 * L.sort_blocks * sizeof(int32_t));
+    L.ends_a = take(ne1 * sizeof(int32_t));
+    L.ends_b = take(ne1 * sizeof(int32_t));
+    L.sort_err = take(sizeof(int32_t));
     L.labels = take(ns * sizeof(int32_t));
     L.sxs = take((size_t)cols * sizeof(int32_t));
     L.sys = take((size_t)rows * sizeof(int32_t));
@@ -194,6 +208,138 @@ __global__ void k_edge_weights(const double* __restrict__ sm, int h, int w, doub
         s = s + d1 * d1;
         s = s + d2 * d2;
         wt[i] = sqrt(s);
+    }
+}
+
+// ------------------------------------------------------------ edge order --
+// The merge visits the edges by ascending weight, equal weights in edge
+// order: a stable LSD radix sort of the weights' IEEE bit patterns (which
+// order non-negative doubles like their values), 8 passes of 8-bit digits,
+// carrying the edge index.  Each pass: per-block digit counts over a chunk
+// of kSortChunk edges, one exclusive scan over (digit, block), then a
+// scatter that ranks equal digits within a warp (match + popc), across the
+// warps of a 256-edge tile and across tiles in order, so the chunk keeps
+// its order within each digit.
+__global__ void k_sort_init(uint32_t* __restrict__ vals, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        vals[i] = (uint32_t)i;
+}
+
+__global__ void __launch_bounds__(256) k_sort_count(const unsigned long long* __restrict__ keys, long long n, int shift,
+                                                    int32_t* __restrict__ counts, int nblocks) {
+    __shared__ int32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const long long base = (long long)blockIdx.x * kSortChunk;
+    for (int i = threadIdx.x; i < kSortChunk; i += 256) {
+        const long long e = base + i;
+        if (e < n) atomicAdd(&h[(keys[e] >> shift) & 255], 1);
+    }
+    __syncthreads();
+    counts[threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+// exclusive scan of counts[0, total) in place; one block of 1024 threads
+__global__ void __launch_bounds__(1024) k_sort_scan(int32_t* __restrict__ counts, int total) {
+    __shared__ int32_t part[1024];
+    const int t = threadIdx.x, per = (total + 1023) / 1024;
+    const int b = min(t * per, total), e = min(b + per, total);
+    int32_t s = 0;
+#pragma unroll 8
+    for (int i = b; i < e; ++i) s += counts[i];
+    part[t] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int32_t v = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int32_t run = t ? part[t - 1] : 0;
+#pragma unroll 8
+    for (int i = b; i < e; ++i) {
+        const int32_t c = counts[i];
+        counts[i] = run;
+        run += c;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_sort_scatter(const unsigned long long* __restrict__ kin,
+                                                      const uint32_t* __restrict__ vin,
+                                                      unsigned long long* __restrict__ kout,
+                                                      uint32_t* __restrict__ vout, long long n, int shift,
+                                                      const int32_t* __restrict__ offsets, int nblocks, int* err) {
+    __shared__ int32_t run[256];         // next slot of each digit for this chunk
+    __shared__ int32_t wcount[8][256];   // per-warp digit counts of the current tile
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    run[t] = offsets[t * nblocks + blockIdx.x];
+    for (int w = 0; w < 8; ++w) wcount[w][t] = 0;
+    __syncthreads();
+    const long long base = (long long)blockIdx.x * kSortChunk;
+    for (int tile = 0; tile < kSortChunk; tile += 256) {
+        const long long e = base + tile + t;
+        const bool valid = e < n;
+        unsigned long long k = 0;
+        uint32_t v = 0;
+        int d = 256;  // past the end: a digit of its own, never written
+        if (valid) {
+            k = kin[e];
+            v = vin[e];
+            d = (int)((k >> shift) & 255);
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && lane == __ffs(peers) - 1) wcount[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            long long pos = (long long)run[d] + rank;
+            for (int w = 0; w < warp; ++w) pos += wcount[w][d];
+            if (pos >= 0 && pos < n) {
+                kout[pos] = k;
+                vout[pos] = v;
+            } else {
+                atomicOr(err, 1);
+            }
+        }
+        __syncthreads();
+        int32_t add = 0;
+        for (int w = 0; w < 8; ++w) {
+            add += wcount[w][t];
+            wcount[w][t] = 0;
+        }
+        run[t] += add;
+        __syncthreads();
+    }
+}
+
+// endpoints of the sorted edges (the groups of k_edge_weights)
+__global__ void k_sorted_ends(const uint32_t* __restrict__ order, long long ne, int h, int w, int32_t* __restrict__ sa,
+                              int32_t* __restrict__ sb) {
+    const long long nr = (long long)h * (w - 1), nd = (long long)(h - 1) * w, ng = (long long)(h - 1) * (w - 1);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ne;
+         i += (long long)gridDim.x * blockDim.x) {
+        long long e = order[i], a, b;
+        if (e >= ne) {  // not a permutation: the sort's own check reports it
+            sa[i] = sb[i] = 0;
+            continue;
+        }
+        if (e < nr) {
+            const long long y = e / (w - 1), x = e % (w - 1);
+            a = y * w + x, b = a + 1;
+        } else if ((e -= nr) < nd) {
+            a = e, b = e + w;
+        } else {
+            e -= nd;
+            const bool up = e >= ng;
+            if (up) e -= ng;
+            const long long y = e / (w - 1), x = e % (w - 1), p = y * w + x;
+            if (up)
+                a = p + 1, b = p + w;
+            else
+                a = p, b = p + w + 1;
+        }
+        sa[i] = (int32_t)a;
+        sb[i] = (int32_t)b;
     }
 }
 
@@ -437,16 +583,46 @@ extern "C" int32_t gmvs_superpixels(const uint8_t* image, const uint8_t* gray, c
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail_cuda(e, who);
 
-    // host: the merge
-    std::vector<double> weights((size_t)std::max<int64_t>(L.ne, 1));
-    std::vector<int32_t> labels((size_t)sh * sw);
+    // the visiting order on the device; endpoints and weights to the host
+    const size_t ne1 = (size_t)std::max<int64_t>(L.ne, 1);
+    std::vector<double> sorted_w(ne1);
+    std::vector<int32_t> ends_a(ne1), ends_b(ne1), labels((size_t)sh * sw);
+    int32_t sort_err = 0;
     if (L.ne > 0) {
-        e = cudaMemcpyAsync(weights.data(), ws + L.weights, sizeof(double) * L.ne, cudaMemcpyDeviceToHost, st);
+        unsigned long long* ka = (unsigned long long*)(ws + L.weights);
+        unsigned long long* kb = (unsigned long long*)(ws + L.keys2);
+        uint32_t* va = (uint32_t*)(ws + L.vals);
+        uint32_t* vb = (uint32_t*)(ws + L.vals2);
+        int32_t* counts = (int32_t*)(ws + L.counts);
+        int* err = (int*)(ws + L.sort_err);
+        e = cudaMemsetAsync(err, 0, sizeof(int), st);
+        if (e != cudaSuccess) return fail_cuda(e, who);
+        k_sort_init<<<grid_1d((size_t)L.ne), 256, 0, st>>>(va, L.ne);
+        for (int pass = 0; pass < 8; ++pass) {  // even: the result ends in ka / va
+            k_sort_count<<<L.sort_blocks, 256, 0, st>>>(ka, L.ne, 8 * pass, counts, L.sort_blocks);
+            k_sort_scan<<<1, 1024, 0, st>>>(counts, 256 * L.sort_blocks);
+            k_sort_scatter<<<L.sort_blocks, 256, 0, st>>>(ka, va, kb, vb, L.ne, 8 * pass, counts, L.sort_blocks, err);
+            std::swap(ka, kb);
+            std::swap(va, vb);
+        }
+        k_sorted_ends<<<grid_1d((size_t)L.ne), 256, 0, st>>>(va, L.ne, sh, sw, (int32_t*)(ws + L.ends_a),
+                                                             (int32_t*)(ws + L.ends_b));
+        e = cudaGetLastError();
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(sorted_w.data(), ka, sizeof(double) * L.ne, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(ends_a.data(), ws + L.ends_a, sizeof(int32_t) * L.ne, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(ends_b.data(), ws + L.ends_b, sizeof(int32_t) * L.ne, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&sort_err, err, sizeof(int), cudaMemcpyDeviceToHost, st);
         if (e != cudaSuccess) return fail_cuda(e, who);
     }
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return fail_cuda(e, who);
-    const int32_t kept = superpixel_labels(sh, sw, weights.data(), P.scale / 255.0, P.min_size, labels.data());
+    if (sort_err) return fail(GMVS_ERR_DEVICE, std::string(who) + ": edge sort produced an out-of-range slot");
+    // host: the merge
+    const int32_t kept = superpixel_merge_sorted(sh, sw, L.ne, ends_a.data(), ends_b.data(), sorted_w.data(),
+                                                 P.scale / 255.0, P.min_size, labels.data());
     if (out_num_segments) *out_num_segments = kept;
     // pageable source: the call returns once the labels are staged
     e = cudaMemcpyAsync(ws + L.labels, labels.data(), sizeof(int32_t) * labels.size(), cudaMemcpyHostToDevice, st);

@@ -12,4 +12,9 @@ namespace gmvs {
 // returns how many segments were kept.
 int32_t superpixel_labels(int rows, int cols, const double* weights, double k, int min_size, int32_t* labels);
 
+// The same from the ne edges already in visiting order (ascending weight,
+// ties in edge order): endpoints sa, sb and weights sw.
+int32_t superpixel_merge_sorted(int rows, int cols, int64_t ne, const int32_t* sa, const int32_t* sb,
+                                const double* sw, double k, int min_size, int32_t* labels);
+
 }  // namespace gmvs
