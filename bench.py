@@ -227,7 +227,7 @@ def segments_run(dev) -> dict:
     return out
 
 
-def superpixels_run(dev, n_images: int = 8, workers: int = 4) -> dict:
+def superpixels_run(dev, n_images: int = 16, workers: int = 8) -> dict:
     """The segmentation preprocessing (extract_superpixel.py seg_func's
     segment-id map) on 1600x1200 BGR images from host memory: one image at a
     time and `workers` at a time (wall clock, host copies included), beside

@@ -239,28 +239,45 @@ __global__ void __launch_bounds__(256) k_sort_count(const unsigned long long* __
     counts[threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
 }
 
-// exclusive scan of counts[0, total) in place; one block of 1024 threads
+// exclusive scan of counts[0, total) in place (total a multiple of 4); one
+// block of 1024 threads walking the array in coalesced rounds of 4096 (four
+// counts per thread, warp scans, a scan of the warp totals, a carry between
+// rounds), the next round's counts loaded while this round is scanned
 __global__ void __launch_bounds__(1024) k_sort_scan(int32_t* __restrict__ counts, int total) {
-    __shared__ int32_t part[1024];
-    const int t = threadIdx.x, per = (total + 1023) / 1024;
-    const int b = min(t * per, total), e = min(b + per, total);
-    int32_t s = 0;
-#pragma unroll 8
-    for (int i = b; i < e; ++i) s += counts[i];
-    part[t] = s;
+    __shared__ int32_t warp_tot[32];
+    __shared__ int32_t carry;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    int4* c4 = reinterpret_cast<int4*>(counts);
+    const int n4 = total / 4;
+    if (t == 0) carry = 0;
     __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        const int32_t v = t >= o ? part[t - o] : 0;
+    int4 next = t < n4 ? c4[t] : make_int4(0, 0, 0, 0);
+    for (int base = 0; base < n4; base += 1024) {
+        const int i = base + t;
+        const int4 v = next;
+        if (i + 1024 < n4) next = c4[i + 1024];
+        const int32_t s = v.x + v.y + v.z + v.w;
+        int32_t x = s;  // inclusive scan of the thread sums within the warp
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[w] = x;
         __syncthreads();
-        part[t] += v;
+        if (w == 0) {
+            int32_t z = warp_tot[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const int32_t y = __shfl_up_sync(0xffffffffu, z, o);
+                if (lane >= o) z += y;
+            }
+            warp_tot[lane] = z;
+        }
         __syncthreads();
-    }
-    int32_t run = t ? part[t - 1] : 0;
-#pragma unroll 8
-    for (int i = b; i < e; ++i) {
-        const int32_t c = counts[i];
-        counts[i] = run;
-        run += c;
+        const int32_t excl = carry + (w ? warp_tot[w - 1] : 0) + (x - s);
+        if (i < n4) c4[i] = make_int4(excl, excl + v.x, excl + v.x + v.y, excl + v.x + v.y + v.z);
+        __syncthreads();
+        if (t == 1023) carry = excl + s;
+        __syncthreads();
     }
 }
 
