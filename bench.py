@@ -420,6 +420,7 @@ def main():
     pipe.run(timed=True)
     stages = dict(pipe.times.seconds)
     sweep_ms, sweep_bytes, launches = sweep_roofline(pipe, torch)
+    samples = ncc_samples_per_step(pipe)
 
     # end-to-end through host buffers: pinned 8-bit images in, fused maps out
     host_imgs = torch.from_numpy(sc.images).pin_memory()
@@ -505,6 +506,7 @@ def main():
                      "launch_ms": sweep_ms,
                      "note": "latency-bound texture/L1 gather, not HBM: ncu shows 36-47 % SM issue, 37 % of the "
                              "texture pipe and under 10 % of DRAM bandwidth"},
+        "ncc_samples": ncc_samples_block(samples, ms, clk.summary()),
         "stages_s": stages,
         "gpu_launches": launches * args.steps,
         "clocks": clk.summary(),
@@ -512,6 +514,32 @@ def main():
         "cpu_baseline": cpu,
     }
     print(json.dumps(out))
+
+
+def ncc_samples_per_step(pipe) -> float:
+    """Algorithmic NCC window samples of one pipeline step: per view and pass
+    H * W * N * 36 * (1 + 14 * I) (the initial costs, then 8 neighbour and
+    5 refinement hypotheses plus the current one per pixel and iteration)."""
+    total = 0.0
+    for key in pipe.plans:
+        for plan in pipe.plans[key]:
+            iters = (plan.num_stages - 4) // 2
+            for v in plan.views:
+                total += v.height * v.width * (len(v.images) - 1) * 36 * (1 + 14 * iters)
+    return total
+
+
+def ncc_samples_block(samples: float, ms: float, clocks: dict) -> dict:
+    """Samples per second and per SM-clock.  A sample costs about 38 warp-lane
+    instructions in the fp16-quad kernels (projection 8, clamp and corner 13,
+    load 3, unpack 2, interpolation 4, weights 1, moments 4, loop 3); an SM
+    issues at most 4 x 32 lane-instructions a clock, so about 3.4 samples per
+    SM-clock is the issue ceiling."""
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    per_s = samples / (ms / 1000.0)
+    per_sm_clk = per_s / (152 * mhz * 1e6)
+    return {"per_step": samples, "per_s": per_s, "per_sm_clock": per_sm_clk, "issue_ceiling_per_sm_clock": 128 / 38,
+            "frac_of_issue_ceiling": per_sm_clk / (128 / 38)}
 
 
 def sweep_roofline(pipe, torch):
