@@ -220,3 +220,26 @@ def test_seg_func_files_and_threads(gmvs_lib, cuda, tmp_path):
     m2, _ = sp.segment_ids(imgs[1][0], imgs[1][1], var_thresh2=0.1)
     m1, _ = sp.segment_ids(imgs[1][0], imgs[1][1])
     assert set(np.unique(m2)) <= set(np.unique(m1))
+
+
+def test_superpixels_rejects_bad_arguments_before_any_device_work(gmvs_lib):
+    """NULL image, missing gray with the variance filter on, bad parameters
+    and a short workspace fail with GMVS_ERR_INVALID before any CUDA call."""
+    from gmvs_gb300 import superpixel as sp
+
+    L = _abi.lib()
+    p = sp.default_params()
+    fake = 1 << 20  # never dereferenced: every case fails validation first
+    big = L.gmvs_superpixel_workspace_bytes(64, 64, ctypes.byref(p))
+    cases = [
+        (None, fake, 64, 64, p, fake, big),          # NULL image
+        (fake, None, 64, 64, p, fake, big),          # filter on, ids_map wanted, no gray
+        (fake, fake, 0, 64, p, fake, big),           # empty image
+        (fake, fake, 64, 64, sp.default_params(close_size=4), fake, big),
+        (fake, fake, 64, 64, p, fake, big // 2),     # workspace too small
+        (fake, fake, 64, 64, p, None, big),          # NULL workspace
+    ]
+    for img, gray, rows, cols, prm, ws, nbytes in cases:
+        rc = L.gmvs_superpixels(img, gray, None, rows, cols, ctypes.byref(prm), None, None, fake, None, None, ws,
+                                nbytes, None)
+        assert rc == _abi.ERR_INVALID, L.gmvs_last_error()
