@@ -478,6 +478,7 @@ def main():
         except (OSError, ValueError):
             traffic = None
     cpu = None if args.no_cpu else cpu_baseline(sc, os.cpu_count() or 1)
+    clocks = clk.summary()  # reads and removes the sample file: once
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -506,10 +507,10 @@ def main():
                      "launch_ms": sweep_ms,
                      "note": "latency-bound texture/L1 gather, not HBM: ncu shows 36-47 % SM issue, 37 % of the "
                              "texture pipe and under 10 % of DRAM bandwidth"},
-        "ncc_samples": ncc_samples_block(samples, ms, clk.summary()),
+        "ncc_samples": ncc_samples_block(samples, ms, clocks),
         "stages_s": stages,
         "gpu_launches": launches * args.steps,
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "plain_path": plain,
         "cpu_baseline": cpu,
     }
