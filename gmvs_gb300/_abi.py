@@ -103,6 +103,16 @@ _SIGS = {
     "gmvs_gather_workspace_bytes": (ctypes.c_size_t, [_i, _i]),
     "gmvs_gather_points": (_i, [_p, _p, _i, _i, _p, _p, _f, _p, _p, _p, _p, _p, _p, ctypes.c_size_t, _p]),
     "gmvs_view_scores": (_i, [_p, _p, _i, _p, _i, _p, _p, _p]),
+    "gmvs_ctx_create": (_i, [_i, ctypes.POINTER(_p)]),
+    "gmvs_ctx_destroy": (None, [_p]),
+    "gmvs_ctx_last_error": (_i, [_p, ctypes.c_char_p, ctypes.c_size_t]),
+    "gmvs_job_create": (_i, [_p, ctypes.POINTER(gmvs_camera), _i, _i, _i, _p, _p, ctypes.POINTER(gmvs_problem), _i,
+                             ctypes.POINTER(_p)]),
+    "gmvs_job_destroy": (None, [_p]),
+    "gmvs_pass_random_prior": (_i, [_p, _p, _i, ctypes.POINTER(gmvs_params), _p]),
+    "gmvs_pass_geom": (_i, [_p, _p, _i, ctypes.POINTER(gmvs_params), _p, _p, _p]),
+    "gmvs_job_fuse": (_i, [_p, _p, _i, _i, _p, _p]),
+    "gmvs_export": (_i, [_p, _i, _i, _p, _p, _p, _p]),
     "gmvs_superpixel_default_params": (None, [ctypes.POINTER(gmvs_superpixel_params)]),
     "gmvs_superpixel_workspace_bytes": (ctypes.c_size_t, [_i, _i, ctypes.POINTER(gmvs_superpixel_params)]),
     "gmvs_superpixel_labels_host": (_i, [_i, _i, _p, ctypes.c_double, _i, _p, _p]),

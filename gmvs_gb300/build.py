@@ -42,6 +42,7 @@ SOURCES = {
     "gather.cu": [],
     "views.cu": [],
     "superpixel.cu": [],
+    "job.cu": [],
     "prior.cpp": [],
     "felzenszwalb.cpp": [],
 }

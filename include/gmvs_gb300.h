@@ -333,6 +333,55 @@ GMVS_API int32_t gmvs_view_scores(const long long* offsets, const int32_t* point
                          const double* xyz, int32_t num_points, const double* centers, float* scores,
                          void* stream);
 
+/* ------------------------------------------------------------ scene jobs --
+ * The reference's whole reconstruction of one scene (launch.py:143-173) for
+ * hosts that are not Python: a job holds the scene's cameras, problems and
+ * images and owns the device state of its passes (it allocates, like
+ * PlanarInit, planar_initer.cu:21-62; the plan API above does not);
+ * gmvs_pass_random_prior runs the random pass, the host triangulation and
+ * the planar-prior pass of planar_init.py:113-190 (PlanarInit::
+ * run_patch_match, triangulation, cuda_planar_prior_init), gmvs_pass_geom
+ * one geometric pass of consistency.py (PatchMatcher::run_patch_match,
+ * gmvs/src/patch_match.cu:1353-1518), gmvs_job_fuse the fusion of every
+ * problem in order (Fuser::run_fusion, gmvs/src/fusion.cu:211-275) with the
+ * normal renormalisation of consistency.py:193-197, and gmvs_export copies
+ * one view's maps out (PlanarInit::export_plane, planar_initer.cu:104-117).
+ * The pass parameters come from the caller's gmvs_params (init / sweep kind,
+ * sampler and pass index are set per pass; the reference's geometric passes
+ * use max_iterations = 2).  Problem sets are indices into `problems`
+ * (NULL = all).  Every call enqueues on `stream`; the prior pass and plan
+ * creation synchronise it.  A context must outlive its jobs. */
+typedef struct gmvs_ctx gmvs_ctx;
+typedef struct gmvs_job gmvs_job;
+
+GMVS_API int32_t gmvs_ctx_create(int32_t device, gmvs_ctx** out);
+GMVS_API void gmvs_ctx_destroy(gmvs_ctx* ctx);
+/* The message of the last failing job call of this context. */
+GMVS_API int32_t gmvs_ctx_last_error(const gmvs_ctx* ctx, char* buf, size_t len);
+/* cams: host [num_images], every one height x width; images: device fp32
+ * [num_images][height][width], caller-owned, kept for the job's life;
+ * superpixels: host uint8 [num_images][height][width] (copied) or NULL =
+ * no superpixel filter in the triangulation; problems: host [num_problems]. */
+GMVS_API int32_t gmvs_job_create(gmvs_ctx* ctx, const gmvs_camera* cams, int32_t num_images, int32_t height,
+                        int32_t width, const float* images, const uint8_t* superpixels,
+                        const gmvs_problem* problems, int32_t num_problems, gmvs_job** out);
+GMVS_API void gmvs_job_destroy(gmvs_job* job);
+GMVS_API int32_t gmvs_pass_random_prior(gmvs_job* job, const int32_t* problem_ids, int32_t n,
+                               const gmvs_params* params, void* stream);
+/* depth_in [V][H][W] / normal_in [V][H][W][3] (device): the maps the pass
+ * starts from, or both NULL = the job's last pass. */
+GMVS_API int32_t gmvs_pass_geom(gmvs_job* job, const int32_t* problem_ids, int32_t n, const gmvs_params* params,
+                       const float* depth_in, const float* normal_in, void* stream);
+/* masks: device bool [V][H][W] the fusion marks (zeroed first), or NULL =
+ * the job's own. */
+GMVS_API int32_t gmvs_job_fuse(gmvs_job* job, const int32_t* order, int32_t n, int32_t geom_consistent,
+                      uint8_t* masks, void* stream);
+/* which: 0 = the last pass (depth, normal, cost), 1 = fused (depth, normal;
+ * cost must be NULL).  Outputs are device or host arrays of one view
+ * ([H][W], [H][W][3], [H][W]); any may be NULL. */
+GMVS_API int32_t gmvs_export(gmvs_job* job, int32_t view, int32_t which, float* depth, float* normal, float* cost,
+                    void* stream);
+
 /* -------------------------------------------------------------- superpixels --
  * The segmentation preprocessing of gmvs/scripts/extract_superpixel.py:
  * extract_superpixel (lines 55-74: resize to seg_cols x seg_rows,
