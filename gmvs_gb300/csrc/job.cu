@@ -98,9 +98,12 @@ int32_t problem_set(const gmvs_job* job, const int32_t* ids, int32_t n, std::vec
         return GMVS_OK;
     }
     if (n < 1) return fail(GMVS_ERR_INVALID, std::string(who) + ": empty problem set");
+    std::vector<char> seen(job->problems.size(), 0);
     for (int32_t i = 0; i < n; ++i) {
         if (ids[i] < 0 || ids[i] >= (int32_t)job->problems.size())
             return fail(GMVS_ERR_INVALID, std::string(who) + ": problem index out of range");
+        if (seen[ids[i]]++)  // one launch may not write a view's maps twice
+            return fail(GMVS_ERR_INVALID, std::string(who) + ": problem listed twice");
         out.push_back(ids[i]);
     }
     return GMVS_OK;
@@ -196,6 +199,13 @@ extern "C" int32_t gmvs_job_create(gmvs_ctx* ctx, const gmvs_camera* cams, int32
             return fail(GMVS_ERR_INVALID, ctx->last_error);
         }
     }
+    std::vector<char> is_ref(num_images, 0);
+    for (int32_t k = 0; k < num_problems; ++k)
+        if (is_ref[problems[k].ref_image_id]++) {
+            ctx->last_error = std::string(who) + ": two problems share reference view " +
+                              std::to_string(problems[k].ref_image_id);
+            return fail(GMVS_ERR_INVALID, ctx->last_error);
+        }
     for (int32_t i = 0; i < num_images; ++i)
         if (cams[i].height != height || cams[i].width != width) {
             ctx->last_error = std::string(who) + ": every camera must be height x width";
