@@ -90,6 +90,13 @@ def test_job_api_equals_python_pipeline(gmvs_lib, cuda):
         assert L.gmvs_export(job, V, 0, d.data_ptr(), None, None, None) == _abi.ERR_INVALID
         assert "no such view" in err()
         assert L.gmvs_export(job, 0, 1, None, None, c.data_ptr(), None) == _abi.ERR_INVALID
+        twice = (ctypes.c_int32 * 2)(0, 0)
+        assert L.gmvs_pass_geom(job, twice, 2, ctypes.byref(g), None, None, None) == _abi.ERR_INVALID
+        assert "twice" in err()
+        shared = (_abi.gmvs_problem * 2)(probs[0], probs[0])
+        other = ctypes.c_void_p()
+        assert L.gmvs_job_create(ctx, cams, V, H, W, images.data_ptr(), None, shared, 2,
+                                 ctypes.byref(other)) == _abi.ERR_INVALID
     finally:
         L.gmvs_job_destroy(job)
         L.gmvs_ctx_destroy(ctx)
