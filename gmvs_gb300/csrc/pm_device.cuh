@@ -262,12 +262,18 @@ __device__ __forceinline__ float ncc_cost(const DevView& V, const DevParams& prm
         const float zc = fmaf(m7, qys[0], bz1), zd = fmaf(m7, qys[NS - 1], bz1);
         const float zlo = fminf(fminf(za, zb), fminf(zc, zd)), zhi = fmaxf(fmaxf(za, zb), fmaxf(zc, zd));
         const bool in_range = (zlo >= kRcpLo && zhi <= kRcpHi) || (zhi <= -kRcpLo && zlo >= -kRcpHi);
-#define GMVS_SAMPLE_COLUMN(RCP, ROWS)                                                              \
+        // QY(bb): the window row's coordinate, from the table where the row
+        // loop is unrolled; computed in place where it is not, so that the
+        // table is never indexed at run time (that would put it in local
+        // memory for every evaluation)
+#define GMVS_QY_TABLE(bb) qys[bb]
+#define GMVS_QY_DIRECT(bb) ((float)window_coord<S>(py, -radius + (bb) * inc, V.H))
+#define GMVS_SAMPLE_COLUMN(RCP, ROWS, QY)                                                          \
     {                                                                                              \
         const float qx = (float)window_coord<S>(px, -radius + (q.h * NC + al) * inc, V.W);        \
         const float bx = fmaf(m0, qx, m2), by = fmaf(m3, qx, m5), bz = fmaf(m6, qx, m8);           \
         _Pragma(ROWS) for (int bb = 0; bb < NS; ++bb) {                                            \
-            const float qy = qys[bb];                                                              \
+            const float qy = QY(bb);                                                               \
             const float rz = RCP(fmaf(m7, qy, bz));                                                \
             const float u = fmaf(m1, qy, bx) * rz;                                                 \
             const float v = fmaf(m4, qy, by) * rz;                                                 \
@@ -284,17 +290,25 @@ __device__ __forceinline__ float ncc_cost(const DevView& V, const DevParams& prm
                 // one instruction per sample: unroll the columns too, so all
                 // of this lane's fetches can be in flight together
 #pragma unroll
-                for (int al = 0; al < NC; ++al) GMVS_SAMPLE_COLUMN(rcp_in_range, "unroll")
+                for (int al = 0; al < NC; ++al) GMVS_SAMPLE_COLUMN(rcp_in_range, "unroll", GMVS_QY_TABLE)
             } else {
                 // software-interpolated samples: keep the code compact
 #pragma unroll 1
-                for (int al = 0; al < NC; ++al) GMVS_SAMPLE_COLUMN(rcp_in_range, "unroll")
+                for (int al = 0; al < NC; ++al) GMVS_SAMPLE_COLUMN(rcp_in_range, "unroll", GMVS_QY_TABLE)
             }
-        } else {
+        } else if constexpr (S::kTex) {
 #pragma unroll 1
-            for (int al = 0; al < NC; ++al) GMVS_SAMPLE_COLUMN(rcp_rn, "unroll 1")
+            for (int al = 0; al < NC; ++al) GMVS_SAMPLE_COLUMN(rcp_rn, "unroll 1", GMVS_QY_DIRECT)
+        } else {
+            // the software samplers keep the table in local memory (measured
+            // faster at their 128-register budget than holding it in registers
+            // across the rolled column loop)
+#pragma unroll 1
+            for (int al = 0; al < NC; ++al) GMVS_SAMPLE_COLUMN(rcp_rn, "unroll 1", GMVS_QY_TABLE)
         }
 #undef GMVS_SAMPLE_COLUMN
+#undef GMVS_QY_TABLE
+#undef GMVS_QY_DIRECT
     } else {
         const int radius = prm.patch_size / 2;
         const int inc = prm.radius_increment;
@@ -876,17 +890,21 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
                 }
             }
             // 15 draws; hits per view (at most 15) counted in 4-bit fields
-            unsigned long long cnt4[2] = {0ull, 0ull};
+            // (two scalars, not an array: a run-time index would put it in local memory)
+            unsigned long long cnt_lo = 0ull, cnt_hi = 0ull;  // views 0-15, 16-31
             for (int d = 0; d < 15; ++d) {
                 const float rp = rng.uniform() - 1.1920928955078125e-07f;  // curand_uniform - FLT_EPSILON
                 for (int v = 0; v < N; ++v)
                     if (VW(v) > rp) {
-                        cnt4[v >> 4] += 1ull << ((v & 15) * 4);
+                        if (v < 16)
+                            cnt_lo += 1ull << (v * 4);
+                        else
+                            cnt_hi += 1ull << ((v - 16) * 4);
                         break;
                     }
             }
             for (int i = 0; i < N; ++i) {
-                const float w = (float)((cnt4[i >> 4] >> ((i & 15) * 4)) & 15ull);
+                const float w = (float)((((i < 16) ? cnt_lo : cnt_hi) >> ((i & 15) * 4)) & 15ull);
                 VW(i) = w;
                 if (w > 0) {
                     temp_sel |= 1u << i;
@@ -928,28 +946,36 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
                     ppl = V.prior_planes[center];
                     depth_prior = depth_from_plane(rc, ppl, px, py);
                     if (mask > 0) {  // patch_match_kernel.cu:1256-1305
-                        float rfc[8];
+                        // FindMaxCostIndex over the restricted costs (0 for
+                        // absent neighbours; ties pick the last index), kept
+                        // as a running maximum rather than an array
+                        float rfc_max = 0.0f;
+                        int max_idx = 0;
+#pragma unroll 1
                         for (int k = 0; k < 8; ++k) {
-                            rfc[k] = 0.0f;
+                            float r = 0.0f;
                             if ((flags >> k) & 1u) {
                                 const float4 qp = NPL(k);
                                 const float dn = depth_from_plane(rc, qp, px, py);
                                 const float ac = ppl.x * qp.x + ppl.y * qp.y + ppl.z * qp.z;
-                                rfc[k] = restricted(pk, FC(k), dn - depth_prior, ac);
+                                r = restricted(pk, FC(k), dn - depth_prior, ac);
+                            }
+                            if (k == 0 || r >= rfc_max) {
+                                rfc_max = r;
+                                max_idx = k;
                             }
                         }
-                        const int max_idx = find_max_idx8(rfc);
                         const float dn = depth_from_plane(rc, cur, px, py);
                         const float ac = ppl.x * cur.x + ppl.y * cur.y + ppl.z * cur.z;
                         const float rcn = restricted(pk, cost_now, dn - depth_prior, ac);
                         if ((flags >> max_idx) & 1u) {
                             const float4 qp = NPL(max_idx);
                             const float db = depth_from_plane(rc, qp, px, py);
-                            if (db >= V.depth_min && db <= V.depth_max && rfc[max_idx] > rcn) {
+                            if (db >= V.depth_min && db <= V.depth_max && rfc_max > rcn) {
                                 depth_now = db;
                                 cur = qp;
                                 cur_cost = FC(max_idx);
-                                restricted_cost = rfc[max_idx];
+                                restricted_cost = rfc_max;
                                 cur_sel = temp_sel;
                             }
                         }

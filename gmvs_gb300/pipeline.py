@@ -140,6 +140,10 @@ class ScenePipeline:
                           **kinds)
         if self.base is not None and kind == "geom" and hasattr(self.base, "geom_max_iterations"):
             p.max_iterations = self.base.geom_max_iterations
+        if kind == "geom" and self.mode == "batched" and not hasattr(self.base, "split_sweep"):
+            # the fp16-quad geometric half-sweeps are faster as two kernels
+            # (same results); the autotuner, when given, decides instead
+            p.split_sweep = 1
         return p
 
     def _passes(self):
