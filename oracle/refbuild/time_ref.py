@@ -60,13 +60,16 @@ def main(nviews: int = 4) -> None:
     p = engine.params_struct(init_kind=_abi.INIT_DEPTH_NORMAL, sweep_kind=_abi.SWEEP_GEOM,
                              sampler=_abi.SAMPLER_CLAMP, staging=_abi.STAGE_AUTO, max_iterations=2, pass_index=2)
     ws = engine.Workspace()
-    engine.run_passes(views()[:1], p, ws)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for v in views():
-        engine.run_passes([v], p, ws)
-    torch.cuda.synchronize()
-    plain_s = time.perf_counter() - t0
+    plain = {}
+    for split in (0, 1):
+        p.split_sweep = split
+        engine.run_passes(views()[:1], p, ws)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for v in views():
+            engine.run_passes([v], p, ws)
+        torch.cuda.synchronize()
+        plain[split] = time.perf_counter() - t0
     batched = {}
     for split in (0, 1):
         p.split_sweep = split
@@ -82,7 +85,8 @@ def main(nviews: int = 4) -> None:
     print(json.dumps({"views": len(problems), "size": "1600x1200", "num_src": len(problems[0][1]),
                       "reference_module_b_ms_per_view": 1000 * ref_s / len(problems),
                       "reference_breakdown_ms_per_view": {k: 1000 * v / len(problems) for k, v in ref_t.items()},
-                      "gmvs_plain_ms_per_view": 1000 * plain_s / len(problems),
+                      "gmvs_plain_ms_per_view": 1000 * plain[0] / len(problems),
+                      "gmvs_plain_split_ms_per_view": 1000 * plain[1] / len(problems),
                       "gmvs_batched_ms_per_view": 1000 * batched[0] / len(problems),
                       "gmvs_batched_split_ms_per_view": 1000 * batched[1] / len(problems)}))
 
