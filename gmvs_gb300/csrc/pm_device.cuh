@@ -949,23 +949,41 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
                     depth_prior = depth_from_plane(rc, ppl, px, py);
                     if (mask > 0) {  // patch_match_kernel.cu:1256-1305
                         // FindMaxCostIndex over the restricted costs (0 for
-                        // absent neighbours; ties pick the last index), kept
-                        // as a running maximum rather than an array
+                        // absent neighbours; ties pick the last index).  The
+                        // texture kernels keep a running maximum (an array
+                        // indexed at run time would sit in local memory); the
+                        // software samplers keep the array, measured faster
+                        // in their single-kernel form.
                         float rfc_max = 0.0f;
                         int max_idx = 0;
+                        if constexpr (S::kTex) {
 #pragma unroll 1
-                        for (int k = 0; k < 8; ++k) {
-                            float r = 0.0f;
-                            if ((flags >> k) & 1u) {
-                                const float4 qp = NPL(k);
-                                const float dn = depth_from_plane(rc, qp, px, py);
-                                const float ac = ppl.x * qp.x + ppl.y * qp.y + ppl.z * qp.z;
-                                r = restricted(pk, FC(k), dn - depth_prior, ac);
+                            for (int k = 0; k < 8; ++k) {
+                                float r = 0.0f;
+                                if ((flags >> k) & 1u) {
+                                    const float4 qp = NPL(k);
+                                    const float dn = depth_from_plane(rc, qp, px, py);
+                                    const float ac = ppl.x * qp.x + ppl.y * qp.y + ppl.z * qp.z;
+                                    r = restricted(pk, FC(k), dn - depth_prior, ac);
+                                }
+                                if (k == 0 || r >= rfc_max) {
+                                    rfc_max = r;
+                                    max_idx = k;
+                                }
                             }
-                            if (k == 0 || r >= rfc_max) {
-                                rfc_max = r;
-                                max_idx = k;
+                        } else {
+                            float rfc[8];
+                            for (int k = 0; k < 8; ++k) {
+                                rfc[k] = 0.0f;
+                                if ((flags >> k) & 1u) {
+                                    const float4 qp = NPL(k);
+                                    const float dn = depth_from_plane(rc, qp, px, py);
+                                    const float ac = ppl.x * qp.x + ppl.y * qp.y + ppl.z * qp.z;
+                                    rfc[k] = restricted(pk, FC(k), dn - depth_prior, ac);
+                                }
                             }
+                            max_idx = find_max_idx8(rfc);
+                            rfc_max = rfc[max_idx];
                         }
                         const float dn = depth_from_plane(rc, cur, px, py);
                         const float ac = ppl.x * cur.x + ppl.y * cur.y + ppl.z * cur.z;
