@@ -40,8 +40,8 @@ def default_params(**overrides) -> gmvs_superpixel_params:
 
 def bgr_to_gray(image: np.ndarray) -> np.ndarray:
     """ITU-R BT.601 luma of a BGR uint8 image, rounded to nearest."""
-    x = image.astype(np.float64)
-    return np.clip(np.rint(0.114 * x[..., 0] + 0.587 * x[..., 1] + 0.299 * x[..., 2]), 0, 255).astype(np.uint8)
+    x = image.astype(np.float64)  # summed in imageio.imread_gray's order: R, G, B
+    return np.clip(np.rint(0.299 * x[..., 2] + 0.587 * x[..., 1] + 0.114 * x[..., 0]), 0, 255).astype(np.uint8)
 
 
 def _device_u8(a, shape, name: str, dev: torch.device) -> torch.Tensor:

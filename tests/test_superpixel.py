@@ -243,3 +243,29 @@ def test_superpixels_rejects_bad_arguments_before_any_device_work(gmvs_lib):
         rc = L.gmvs_superpixels(img, gray, None, rows, cols, ctypes.byref(prm), None, None, fake, None, None, ws,
                                 nbytes, None)
         assert rc == _abi.ERR_INVALID, L.gmvs_last_error()
+
+
+def test_read_bgr_and_gray_conversion(tmp_path):
+    """cv2.imread's BGR order and gray images read back as three equal
+    channels; the gray conversion is BT.601 rounded, as imread_gray."""
+    from gmvs_gb300 import superpixel as sp
+    from gmvs_gb300.imageio import imread_gray, write_png
+
+    rng = np.random.default_rng(9)
+    rgb = rng.integers(0, 256, (13, 17, 3)).astype(np.uint8)
+    p = os.path.join(tmp_path, "c.png")
+    write_png(p, rgb)
+    bgr = sp.read_bgr(p)
+    assert np.array_equal(bgr, rgb[..., ::-1])
+    assert np.array_equal(sp.bgr_to_gray(bgr), imread_gray(p))
+    g = rng.integers(0, 256, (9, 11)).astype(np.uint8)
+    q = os.path.join(tmp_path, "g.png")
+    write_png(q, g)
+    assert np.array_equal(sp.read_bgr(q), np.repeat(g[..., None], 3, axis=2))
+
+
+def test_extract_superpixel_rejects_weights():
+    from gmvs_gb300 import superpixel as sp
+
+    with pytest.raises(NotImplementedError):
+        sp.extract_superpixel(np.zeros((4, 4, 3), np.uint8), weight=np.ones((4, 4, 3)))
