@@ -42,6 +42,10 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-view comparison step")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-serving", action="store_true", help="skip the served-stream latency measurement")
+    ap.add_argument("--serving-full", action="store_true",
+                    help="serve the full rate sweep (0.5, 1, 2, 4 jobs/s, 6 jobs each) with the plain-path denominator")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip timing the reference's own plain per-view GPU path")
     ap.add_argument("--batching", action="store_true",
                     help="measure the batching form instead: reference views of uneven size and source count "
                          "from four scenes, one launch per stage against one launch chain per view")
@@ -114,59 +118,259 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ CPU baseline --
-def cpu_baseline(sc, threads: int):
-    """The oracle's multi-view NCC evaluation of one full 1600x1200 reference
-    view with 10 sources, timed on the host cores; a pipeline reference view
-    costs 144 such evaluations (random and prior passes 1 + 14*3 each, two
-    geometric passes 1 + 14*2 each), which gives ref-views/s."""
+CPU_SAMPLE_HW = (120, 160)
+
+
+def cpu_pipeline_sample(threads: int, seed: int = 0) -> dict:
+    """One bounded sample of the workload on the host cores, through the
+    oracle (the CPU restatement of the reference path; the reference itself
+    has no CPU implementation of these passes): the room scene rendered at
+    160x120 (same geometry and cameras, intrinsics scaled), reference view 0
+    with its 10 sources through the whole per-view pipeline -- random pass
+    (init, 3 iterations, filter), triangulation prior, prior pass, two
+    geometric passes (the sources' depth maps: ground truth with 0.5 % noise)
+    and fusion.  Every pixel costs the same NCC work as at 1600x1200
+    (36 samples x hypotheses x sources), so the sample is 1/100 of a
+    1600x1200 reference view; ref-views/s scales by that pixel ratio only."""
     import numpy as np
 
     import oracle
+    from gmvs_gb300 import synthetic
+
+    H, W = CPU_SAMPLE_HW
+    sc = synthetic.room_scene(seed, H=H, W=W, num_views=20)
+    ref, src = sc.problems[0]
+    ids = [ref] + list(src)
+    cams = [synthetic.camera_args(sc, i) for i in ids]
+    imgs = sc.images[ids].astype(np.float32)
+    dmin, dmax = sc.depth_range[0] * 0.6, sc.depth_range[1] * 1.2
+    rng = np.random.default_rng(1)
+    nd = (sc.depths[ids] * (1.0 + rng.normal(0, 0.005, (len(ids), H, W)))).astype(np.float32)
+    nn = sc.normals[ids] + rng.normal(0, 0.02, (len(ids), H, W, 3))
+    nn = (nn / np.linalg.norm(nn, axis=-1, keepdims=True)).astype(np.float32)
+    mk = lambda **kw: oracle.make_params(depth_min=dmin, depth_max=dmax, stream_id=ref, **kw)
+    t0 = time.perf_counter()
+    d, n, c, planes = oracle.run_pass(cams, imgs, mk(sampler=1), nthreads=threads)
+    pp, pm, _ = oracle.build_prior(cams[0], d, c, sc.superpixels[ref], True, dmin, dmax)
+    d, n, c, _ = oracle.run_pass(cams, imgs, mk(sampler=1, init_kind=1, sweep_kind=1, pass_index=1), prior_planes=pp,
+                                 prior_masks=pm, init_planes=planes, init_costs=c, nthreads=threads)
+    for g in range(2):
+        nd[0], nn[0] = d, n
+        d, n, c, _ = oracle.run_pass(cams, imgs, mk(sampler=0, init_kind=2, sweep_kind=2, max_iterations=2,
+                                                     pass_index=2 + g), depths=nd, ref_normal=nn[0],
+                                     nthreads=threads)
+    nd[0], nn[0] = d, n
+    masks = np.zeros((sc.num_views, H, W), np.uint8)
+    oracle.fuse(cams, ref, src, nd, nn, masks, 3)
+    dt = time.perf_counter() - t0
+    frac = (H * W) / (1200 * 1600)
+    return {"value": frac / dt, "unit": UNIT, "cores": threads, "kind": "port", "seconds": dt,
+            "sample": f"oracle pipeline of one reference view of the room scene at {W}x{H} (10 sources: random "
+                      f"pass, prior, prior pass, 2 geometric passes, fusion) = {frac:.4f} of a 1600x1200 view"}
+
+
+def fp64_baseline(threads: int) -> dict:
+    """The FP64 CPU oracle: one full multi-view cost evaluation plus one
+    propagation half-sweep with every NCC in double precision, on the plain
+    small configuration (320x256, 4 sources) and on one 1600x1200 room view
+    (10 sources)."""
+    import numpy as np
+
+    import oracle
+    from gmvs_gb300 import synthetic
+
+    out = {"cores": threads, "nproc": os.cpu_count()}
+    for name, sc in (("config1_320x256_4src", synthetic.small_scene(0)),
+                     ("room_1600x1200_10src", synthetic.room_scene(0, H=1200, W=1600, num_views=20))):
+        ref, src = sc.problems[0]
+        ids = [ref] + list(src)
+        p = oracle.make_params(sampler=0, depth_min=sc.depth_range[0] * 0.6, depth_max=sc.depth_range[1] * 1.2,
+                               max_iterations=1, max_half_sweeps=1, fp64=1, run_filter=0)
+        t0 = time.perf_counter()
+        oracle.run_pass([synthetic.camera_args(sc, i) for i in ids], sc.images[ids].astype(np.float32), p,
+                        nthreads=threads)
+        out[name] = {"seconds": time.perf_counter() - t0, "pixels": sc.hw[0] * sc.hw[1], "sources": len(src)}
+    return out
+
+
+# ------------------------------------------- the reference's own GPU path --
+def reference_gpu_run(sc, geom_iters: int = 2, gc: int = 3) -> dict:
+    """The reference's plain per-view GPU path on the same scene, on its own
+    kernels (compiled from its sources by oracle/refbuild/build_ref.py:
+    module A gmvs/lib/src/patch_match_kernel.cu, module B gmvs/src/
+    patch_match.cu and fusion.cu) launched by oracle/refbuild/ref_harness.py
+    with the reference's launch sequences, one reference view at a time,
+    every kernel followed by a device synchronisation and every view's
+    inputs uploaded from host memory, as launch.py drives it:
+      planar_init.initialization per view: PlanarInit's texture upload,
+        random pass, export, triangulation, prior upload, prior pass, export
+        (the triangulation is this build's host prior builder standing in for
+        the reference's, whose cv::Subdiv2D needs OpenCV);
+      consistency.run_patch_match x geom_iters: PatchMatcher per view;
+      consistency.run_fusion: Fuser per view, in order.
+    Host wall clock (the reference synchronises after every launch)."""
+    import numpy as np
+
+    from gmvs_gb300 import engine, synthetic
+    from gmvs_gb300.planar_initer import build_planar_prior
+    from oracle.refbuild import ref_harness as rh
+
+    drv = rh.Driver()
+    V = sc.num_views
+    H, W = sc.hw
+    imgs = sc.images.astype(np.float32)
+    cams = [rh.camera(*synthetic.camera_args(sc, i)) for i in range(V)]
+    gcams = [engine.make_camera(*synthetic.camera_args(sc, i)) for i in range(V)]
+    depth = np.zeros((V, H, W), np.float32)
+    normal = np.zeros((V, H, W, 3), np.float32)
+    st = {"random_pass": 0.0, "triangulation": 0.0, "prior_pass": 0.0, "geom_passes": 0.0, "fusion": 0.0}
+    # warm the modules and the driver on a small case
+    warm = rh.PlanarInitRef(drv, [cams[0], cams[1]], imgs[[0, 1], :64, :64])
+    warm.close()
+    t_all = time.perf_counter()
+    for ref, src in sc.problems:
+        ids = [ref] + list(src)
+        t0 = time.perf_counter()
+        run = rh.PlanarInitRef(drv, [cams[i] for i in ids], imgs[ids])
+        run.run_patch_match(3, planar_prior=False)
+        d, n, c = run.export_plane()
+        t1 = time.perf_counter()
+        dmin, dmax = run.params.depth_min, run.params.depth_max
+        pp, pm, _ = build_planar_prior(gcams[ref], d, c, sc.superpixels[ref], True, dmin, dmax)
+        t2 = time.perf_counter()
+        run.planar_prior_init(pp, pm)
+        run.run_patch_match(3, planar_prior=True)
+        depth[ref], normal[ref], _ = run.export_plane()
+        run.close()
+        t3 = time.perf_counter()
+        st["random_pass"] += t1 - t0
+        st["triangulation"] += t2 - t1
+        st["prior_pass"] += t3 - t2
+    for _ in range(geom_iters):
+        t0 = time.perf_counter()
+        nd, nn = np.empty_like(depth), np.empty_like(normal)
+        for ref, src in sc.problems:
+            nd[ref], nn[ref], _ = rh.run_patch_match(drv, cams, ref, src, imgs, depth, normal, 2)
+        depth, normal = nd, nn
+        st["geom_passes"] += time.perf_counter() - t0
+    t0 = time.perf_counter()
+    rh.run_fusion(drv, cams, sc.problems, depth, normal, gc)
+    st["fusion"] = time.perf_counter() - t0
+    total = time.perf_counter() - t_all
+    return {"value": len(sc.problems) / total, "unit": UNIT, "s_per_step": total, "stages_s": st,
+            "views": len(sc.problems),
+            "kind": "the reference's own kernels (modules A and B compiled from its sources for sm_103a, module A "
+                    "with its --use_fast_math flags) launched with its per-view launch sequences; host "
+                    "triangulation: this build's prior builder in place of the reference's OpenCV one"}
+
+
+# -------------------------------------------------------------- precision --
+def precision_run(sc, dev, pipe, plain_fused) -> dict:
+    """Per-result error statement of the precision form: the fp16-staged
+    NCC (texel quads, fp32 moments, FP64 homography constants) against the
+    FP64 oracle on reference view 0 (half ground-truth, half random
+    hypotheses), reported on a seeded 1 % pixel sample and over the whole
+    view; and the fused maps of the fp16-staged batched pipeline against
+    the fp32 plain per-view pipeline."""
+    import numpy as np
+    import torch
+
+    import oracle
+    from gmvs_gb300 import _abi, engine, synthetic
 
     ref, src = sc.problems[0]
     ids = [ref] + list(src)
-    from gmvs_gb300 import synthetic
-
-    cam_args = [synthetic.camera_args(sc, i) for i in ids]
     H, W = sc.hw
+    rng = np.random.default_rng(0)
     K, R = sc.K[ref], sc.R[ref]
     d = sc.depths[ref].astype(np.float64)
     ys, xs = np.mgrid[0:H, 0:W]
     X = np.stack([(xs - K[0, 2]) / K[0, 0] * d, (ys - K[1, 2]) / K[1, 1] * d, d], -1)
     n = sc.normals[ref].astype(np.float64) @ R.T
-    planes = np.concatenate([n, -np.sum(n * X, -1)[..., None]], -1).astype(np.float32)
-    imgs = sc.images[ids].astype(np.float32)
-    prm = oracle.make_params(sampler=0)
-    oracle.ncc_costs(cam_args, imgs[:, :64], planes[:64], prm, nthreads=threads)  # warm the library
-    t0 = time.perf_counter()
-    oracle.ncc_costs(cam_args, imgs, planes, prm, nthreads=threads)
-    dt = time.perf_counter() - t0
-    evals_per_view = 2 * (1 + 14 * 3) + 2 * (1 + 14 * 2)
-    return {"value": 1.0 / (evals_per_view * dt), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"oracle fp32 multi-view NCC of one {W}x{H} view x {len(src)} sources "
-                      f"({dt:.2f} s) x {evals_per_view} evaluations per pipeline view"}
+    gt = np.concatenate([n, -np.sum(n * X, -1)[..., None]], -1)
+    rd = rng.uniform(0.3, 12.0, (H, W))
+    rn = rng.normal(size=(H, W, 3))
+    rn /= np.linalg.norm(rn, axis=-1, keepdims=True)
+    Xr = X / np.maximum(d[..., None], 1e-9) * rd[..., None]
+    rn[np.sum(rn * Xr, -1) > 0] *= -1
+    rp = np.concatenate([rn, -np.sum(rn * Xr, -1)[..., None]], -1)
+    planes = np.where(rng.random((H, W))[..., None] < 0.5, gt, rp).astype(np.float32)
+    imgs = torch.from_numpy(sc.images[ids].astype(np.float32)).to(dev)
+    v = engine.ViewInputs(cams=[engine.make_camera(*synthetic.camera_args(sc, i)) for i in ids],
+                          images=[imgs[k] for k in range(len(ids))], depth_min=sc.depth_range[0] * 0.6,
+                          depth_max=sc.depth_range[1] * 1.2, stream_id=ref)
+    p = engine.params_struct(sampler=_abi.SAMPLER_CLAMP, staging=_abi.STAGE_QUAD_F16)
+    c16, _, _ = engine.ncc_costs(v, p, torch.from_numpy(planes).to(dev), engine.Workspace(dev))
+    c16 = c16.cpu().numpy()
+    c64, _, _ = oracle.ncc_costs([synthetic.camera_args(sc, i) for i in ids], sc.images[ids].astype(np.float32),
+                                 planes, oracle.make_params(sampler=0), fp64=True)
+    err = np.abs(c16 - c64)
+    pick = rng.random((H, W)) < 0.01
+    out = {"ncc_vs_fp64": {"sample_1pct": {"max": float(err[:, pick].max()), "mean": float(err[:, pick].mean()),
+                                           "pixels": int(pick.sum()), "sources": len(src)},
+                           "whole_view": {"max": float(err.max()), "mean": float(err.mean()),
+                                          "frac_within_1e-3": float(np.mean(err <= 1e-3)),
+                                          "frac_within_1e-4": float(np.mean(err <= 1e-4))},
+                           "staging": "fp16 texel quads, fp32 moments, FP64 homography constants",
+                           "hypotheses": "room view 0, half ground truth, half random"}}
+    if plain_fused is not None:
+        bd, bn = pipe.fused_depth, pipe.fused_normal
+        pd, pn = plain_fused
+        out["fused_vs_fp32_plain"] = {"depth_bit_equal": float((bd == pd).float().mean().item()),
+                                      "normal_bit_equal": float((bn == pn).all(-1).float().mean().item())}
+    return out
 
 
 # ------------------------------------------------------------------ main --
-def serving_run(dev) -> dict:
-    """A bounded served stream: 6 room-scene jobs of 8-12 views at 640x480 to
-    1600x1200 with 4-10 sources, Poisson arrivals at 2 jobs/s, continuous
-    batching with two jobs in flight under the default memory budget."""
+SERVE_SIZES = ((480, 640), (960, 1280), (1200, 1600), (1800, 2400), (2400, 3200))
+
+
+def serving_run(dev, rates=(0.5, 4.0), num_jobs: int = 3, seed: int = 5, views=(8, 50), src=(4, 12),
+                sizes=SERVE_SIZES, plain: bool = False) -> dict:
+    """The serving form: for each arrival rate, a Poisson stream of
+    `num_jobs` room-scene jobs with view counts, resolutions and source
+    counts drawn from `views`, `sizes` and `src` (seeded), served with
+    continuous batching (two jobs in flight, admission by device footprint).
+    Per rate: p50/p99 per-view latency (arrival to fused maps on the host)
+    and sustained ref-views/s.  With `plain`, the same jobs also run one
+    after another through this build's plain per-view path, the
+    denominator of the served throughput."""
     import torch
 
     from gmvs_gb300 import serving
+    from gmvs_gb300.pipeline import SceneInputs, ScenePipeline
 
-    jobs = serving.poisson_stream(6, 2.0, seed=5, views=(8, 12), src=(4, 10), device=dev)
-    torch.cuda.synchronize()
-    srv = serving.ReconstructionServer(device=dev, max_active=2, prior_threads=min(16, os.cpu_count() or 1))
-    for j in jobs:
-        srv.submit(j)
-    srv.run()
-    srv.close()
-    st = serving.latency_stats(jobs)
-    st.update({"jobs": len(jobs), "rate_jobs_per_s": 2.0, "errors": sum(j.error is not None for j in jobs),
-               "mix": [f"{j.num_views}x{j.images.shape[1]}x{j.images.shape[2]}" for j in jobs]})
-    return st
+    out = {"views_per_job": list(views), "sources": list(src),
+           "sizes": [f"{w}x{h}" for h, w in sizes], "slots": 2, "rates": {}}
+    for k, rate in enumerate(rates):
+        jobs = serving.poisson_stream(num_jobs, rate, seed=seed + k, sizes=sizes, views=views, src=src, device=dev)
+        torch.cuda.synchronize()
+        srv = serving.ReconstructionServer(device=dev, max_active=2, prior_threads=min(16, os.cpu_count() or 1))
+        for j in jobs:
+            srv.submit(j)
+        srv.run()
+        srv.close()
+        st = serving.latency_stats(jobs)
+        st.update({"jobs": len(jobs), "errors": sum(j.error is not None for j in jobs),
+                   "mix": [f"{j.num_views}x{j.images.shape[2]}x{j.images.shape[1]}" for j in jobs]})
+        if plain:
+            t0 = time.perf_counter()
+            refs = 0
+            for j in jobs:
+                imgs = torch.from_numpy(j.images).to(dev).float()
+                pp = ScenePipeline(SceneInputs(images=imgs, cams=j.cams, problems=j.problems,
+                                               superpixels=j.superpixels), mode="plain",
+                                   prior_threads=min(16, os.cpu_count() or 1))
+                pp.run()
+                pp.fused_depth.cpu()
+                pp.close()
+                refs += len(j.problems)
+                del pp, imgs
+            st["plain_ref_views_per_s"] = refs / (time.perf_counter() - t0)
+        out["rates"][str(rate)] = st
+        del jobs
+        torch.cuda.empty_cache()
+    return out
 
 
 def job_time_ms(ms: float, world: int, device) -> float:
@@ -262,23 +466,20 @@ def superpixels_run(dev, n_images: int = 16, workers: int = 8) -> dict:
 BATCH_SIZES = ((480, 640), (960, 1280), (1200, 1600), (1800, 2400), (2400, 3200))
 
 
-def batching_run(dev, n_views: int = 16, seed: int = 0, sizes=BATCH_SIZES) -> dict:
-    """Batching form: n_views reference views drawn from four room scenes
-    (seeds 0-3), each scene at a resolution drawn from `sizes` (H, W), 4-12
-    sources per view; the random pass (init + 3 iterations) as one launch
-    per stage over all of them, and as one launch chain per view,
-    CUDA-event timed on one stream."""
+def batching_views(dev, n_views: int = 64, seed: int = 0, sizes=BATCH_SIZES):
+    """n_views reference views drawn from four room scenes (seeds 0-3), each
+    scene at a resolution drawn from `sizes` (H, W), 4-12 sources per view."""
     import numpy as np
     import torch
 
-    from gmvs_gb300 import _abi, engine, synthetic
+    from gmvs_gb300 import engine, synthetic
 
     rng = np.random.default_rng(seed)
     views, mix = [], []
     per_scene = n_views // 4
     for sd in range(4):
         H, W = sizes[int(rng.integers(len(sizes)))]
-        sc = synthetic.room_scene(sd, H=H, W=W, num_views=16, num_src=12, device=dev)
+        sc = synthetic.room_scene(sd, H=H, W=W, num_views=max(16, per_scene), num_src=12, device=dev)
         imgs = torch.from_numpy(sc.images.astype(np.float32)).to(dev)
         cams = [engine.make_camera(*synthetic.camera_args(sc, i)) for i in range(sc.num_views)]
         for ref, src in sc.problems[:per_scene]:
@@ -290,33 +491,66 @@ def batching_run(dev, n_views: int = 16, seed: int = 0, sizes=BATCH_SIZES) -> di
             v.allocate_outputs()
             views.append(v)
             mix.append(f"{W}x{H}/{len(ids) - 1}")
-    p = engine.params_struct(sampler=_abi.SAMPLER_TEX)
+    return views, mix
+
+
+def batching_run(dev, n_views: int = 64, stride: int = 2, seed: int = 0, sizes=BATCH_SIZES) -> dict:
+    """Batching form: the random pass (init, 3 iterations, filter) over
+    n_views uneven reference views (batching_views) with the window stride
+    `stride`, its launch shape picked by the autotuner (tile shapes 16x8,
+    16x16, 32x8, 32x16 pixels, single or split half-sweeps; tuned on four of
+    the views, cached under the stride's own key); then, with that shape,
+    one persistent launch per stage over all views replayed from a CUDA
+    graph against one launch chain per view, CUDA-event timed on one stream."""
+    import torch
+
+    from gmvs_gb300 import _abi, engine
+    from gmvs_gb300.autotune import Autotuner
+
+    views, mix = batching_views(dev, n_views, seed, sizes)
+    p = engine.params_struct(sampler=_abi.SAMPLER_TEX, radius_increment=stride)
+    tuner = Autotuner(reps=1, max_views=4)
+    res = tuner.tune(views, p)
+    p = res.apply(p)
     ws = engine.Workspace(dev)
     batched = engine.Plan(views, p, ws)
     singles = [engine.Plan([v], p, engine.Workspace(dev)) for v in views]
-    st = torch.cuda.current_stream()
+    st = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(st):
+        batched.launch(st)  # first launch: stages the images
+        st.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=st, capture_error_mode="thread_local"):
+            batched.launch(st)
 
     def timed(fn):
         fn()
-        torch.cuda.synchronize()
+        st.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
         fn()
         e1.record(st)
-        torch.cuda.synchronize()
+        st.synchronize()
         return e0.elapsed_time(e1)
 
-    ms_batched = timed(lambda: batched.launch(st))
-    batched_depth = [v.out_depth.clone() for v in views]
-    ms_single = timed(lambda: [pl.launch(st) for pl in singles])
+    with torch.cuda.stream(st):
+        ms_graph = timed(graph.replay)
+        batched_depth = [v.out_depth.clone() for v in views]
+        ms_single = timed(lambda: [pl.launch(st) for pl in singles])
     # the batched launch and the per-view chains compute one thing
     same = all(torch.equal(a, v.out_depth) for a, v in zip(batched_depth, views))
     px = sum(v.height * v.width for v in views)
+    del graph
     for pl in singles + [batched]:
         pl.close()
-    return {"views": len(views), "megapixels": round(px / 1e6, 2), "mix": mix,
-            "random_pass_ms_one_launch_per_stage": ms_batched, "random_pass_ms_one_chain_per_view": ms_single,
-            "speedup": ms_single / ms_batched, "outputs_equal": same}
+    shape = {"tile_w": (res.best[3] if len(res.best) > 3 else 0) or 16, "tile_h_px": 2 * res.best[0],
+             "split_sweep": res.best[2] if len(res.best) > 2 else 0}
+    return {"views": len(views), "stride": stride, "megapixels": round(px / 1e6, 2), "mix": mix,
+            "tuned_shape": shape, "tuning_ms": res.ms,
+            "random_pass_ms_one_launch_per_stage_graph": ms_graph, "random_pass_ms_one_chain_per_view": ms_single,
+            "ref_views_per_s_batched": len(views) / (ms_graph / 1000.0),
+            "ref_views_per_s_per_view_chains": len(views) / (ms_single / 1000.0),
+            "speedup": ms_single / ms_graph, "outputs_equal": same}
 
 
 def main():
@@ -328,28 +562,32 @@ def main():
     if args.batching:
         if rank == 0:
             dev = torch.device("cuda", local)
-            print(json.dumps({"batching_form": {"all_sizes": batching_run(dev),
-                                                "small_sizes": batching_run(dev, sizes=BATCH_SIZES[:2])}}))
+            print(json.dumps({"batching_form": {"stride2_64views": batching_run(dev),
+                                                "stride1_16views": batching_run(dev, n_views=16, stride=1),
+                                                "small_sizes": batching_run(dev, n_views=64,
+                                                                            sizes=BATCH_SIZES[:2])}}))
         return
 
     if args.impl == "reference":
+        # the reference's CPU path: the oracle port (the reference has no CPU
+        # implementation of these passes), one bounded sample per step on all
+        # host cores; rank 0 only
         if rank != 0:
             return
-        from gmvs_gb300 import synthetic
-
-        sc = synthetic.room_scene(0, H=args.height, W=args.width, num_views=args.views,
-                                  device=torch.device("cuda") if torch.cuda.is_available() else None)
         threads = os.cpu_count() or 1
-        vals = []
-        for _ in range(max(1, args.steps)):
-            vals.append(cpu_baseline(sc, threads))
-        v = statistics.median([x["value"] for x in vals])
+        for _ in range(args.warmup):
+            cpu_pipeline_sample(threads)
+        vals = [cpu_pipeline_sample(threads) for _ in range(max(1, args.steps))]
+        sec = statistics.median([x["seconds"] for x in vals])
         cb = dict(vals[0])
-        cb["value"] = v
+        cb["value"] = statistics.median([x["value"] for x in vals])
+        cb["seconds"] = sec
+        v = cb["value"]
         out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-               "warmup": args.warmup, "ms_per_step": 1000.0 / v * args.views, "higher_is_better": True,
+               "warmup": args.warmup, "ms_per_step": 1000.0 * sec, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-               "config": {"workload": WORKLOAD, "views": args.views, "height": args.height, "width": args.width},
+               "config": {"workload": WORKLOAD, "views": args.views, "height": args.height, "width": args.width,
+                          "step": "one bounded sample: " + cb["sample"]},
                "impl": "reference", "cpu_baseline": cb,
                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(out))
@@ -440,7 +678,7 @@ def main():
     torch.cuda.synchronize()
     e2e_ms = e2.elapsed_time(e3) / args.steps
 
-    plain = None
+    plain = pp_fused = None
     if not args.no_plain and rank == 0:
         pp = ScenePipeline(inputs, mode="plain", prior_threads=min(16, os.cpu_count() or 1))
         pp.run()
@@ -450,12 +688,20 @@ def main():
         torch.cuda.synchronize()
         plain_s = time.perf_counter() - t0
         plain = {"value": args.views / plain_s, "unit": UNIT, "steps": 1,
-                 "mode": "one view per launch chain, fp32 images, synchronised after every kernel"}
+                 "mode": "this build's kernels one view per launch chain, fp32 images, synchronised after every "
+                         "kernel"}
+        pp_fused = (pp.fused_depth.clone(), pp.fused_normal.clone())
         pp.close()
+
+    ref_gpu = None
+    if not args.no_reference_gpu and rank == 0:
+        ref_gpu = reference_gpu_run(sc)
+    precision = precision_run(sc, dev, pipe, pp_fused) if rank == 0 else None
 
     served = None
     if not args.no_serving and rank == 0:
-        served = serving_run(dev)
+        served = serving_run(dev, rates=(0.5, 1.0, 2.0, 4.0), num_jobs=6, plain=True) if args.serving_full \
+            else serving_run(dev)
     segments = segments_run(dev) if rank == 0 else None
     superpixels = superpixels_run(dev) if rank == 0 else None
 
@@ -477,7 +723,10 @@ def main():
             traffic = json.load(open(tp)).get("bytes_per_launch")
         except (OSError, ValueError):
             traffic = None
-    cpu = None if args.no_cpu else cpu_baseline(sc, os.cpu_count() or 1)
+    cpu = fp64 = None
+    if not args.no_cpu:
+        cpu = cpu_pipeline_sample(os.cpu_count() or 1)
+        fp64 = fp64_baseline(os.cpu_count() or 1)
     clocks = clk.summary()  # reads and removes the sample file: once
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -487,14 +736,17 @@ def main():
                    "num_src": 10, "parallelism": f"replicas x{world}", "l2": "inputs larger than L2, no flush",
                    "cuda_graphs": True,
                    "launch_shapes": {k: {"tile_h": r.best[0], "ctas_per_sm": r.best[1],
-                                         "split_sweep": r.best[2] if len(r.best) > 2 else 0}
+                                         "split_sweep": r.best[2] if len(r.best) > 2 else 0,
+                                         "tile_w": (r.best[3] if len(r.best) > 3 else 0) or 16}
                                      for k, r in pipe.tuned.items()}},
         "e2e": {"value": world * args.views / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         # pixels x source views evaluated per second (H * W * N * ref-views/s)
         "mpix_views_per_s": value * args.height * args.width * 10 / 1e6,
-        "latency": ({"p50_ms_per_view": served["p50_ms"], "p99_ms_per_view": served["p99_ms"],
-                     "note": "served Poisson stream (see serving): arrival to fused maps on the host, per view"}
+        "latency": ({"p50_ms_per_view": max(r["p50_ms"] for r in served["rates"].values()),
+                     "p99_ms_per_view": max(r["p99_ms"] for r in served["rates"].values()),
+                     "note": "served Poisson streams (see serving), the slowest rate: arrival to fused maps on "
+                             "the host, per view"}
                     if served else
                     {"p50_ms_per_view": ms / args.views, "p99_ms_per_view": ms / args.views,
                      "note": "batched: every view of the scene completes with the step"}),
@@ -512,7 +764,15 @@ def main():
         "gpu_launches": launches * args.steps,
         "clocks": clocks,
         "plain_path": plain,
+        "reference_gpu": ref_gpu,
+        "speedup_vs_reference_gpu": ({"value": value / ref_gpu["value"],
+                                      "e2e": world * args.views / (e2e_ms / 1000.0) / ref_gpu["value"],
+                                      "note": "batched path (images resident / through host buffers) over the "
+                                              "reference's plain per-view GPU path, same scene and box"}
+                                     if ref_gpu else None),
+        "precision": precision,
         "cpu_baseline": cpu,
+        "fp64_cpu_baseline": fp64,
     }
     print(json.dumps(out))
 

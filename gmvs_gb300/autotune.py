@@ -1,16 +1,17 @@
 """Launch-shape autotuner for the PatchMatch kernels.
 
-The knobs that change speed but not results are the tile height (a tile is
-16 pixel columns by 2 * tile_h rows; tile_h thread rows of one warp each per
-CTA, so tile_h = 8 is a 16 x 16 tile and 4 a 16 x 8 tile), the resident
-CTAs per SM (fewer CTAs leave more of the 256 KB of L1/shared memory to the
-sample cache, more CTAs hide more latency) and whether each half-sweep runs
-as one kernel or as two (neighbour hypotheses, then view selection and
-refinement: fewer live registers per kernel, at the price of a per-pixel
-scratch in the workspace).  The window stride
-(radius_increment) is a parameter of the method -- stride 1 and 2 give
-different costs -- so it is not tuned: each stride is tuned on its own and
-keyed separately.
+The knobs that change speed but not results are the tile shape (a tile is
+16 pixel columns by 2 * tile_h rows, tile_h thread rows of one warp each per
+CTA, so tile_h = 8 is a 16 x 16 pixel tile and 4 a 16 x 8 tile; tile_w = 32
+orders the work as 32-pixel-wide blocks of two such tiles, so the shapes
+tried are 16 x 8, 16 x 16, 32 x 8 and 32 x 16 pixels), the resident CTAs per
+SM (fewer CTAs leave more of the 256 KB of L1/shared memory to the sample
+cache, more CTAs hide more latency) and whether each half-sweep runs as one
+kernel or as two (neighbour hypotheses, then view selection and refinement:
+fewer live registers per kernel, at the price of a per-pixel scratch in the
+workspace).  The window stride (radius_increment) is a parameter of the
+method -- stride 1 and 2 give different costs -- so it is not tuned: each
+stride is tuned on its own and keyed separately.
 
 A tuning run times whole plan launches (init, every half-sweep, filter) of a
 representative subset of the batch's views with CUDA events and keeps the
@@ -33,13 +34,15 @@ import torch
 from . import _abi
 from .engine import Plan, ViewInputs, Workspace
 
-TILE_HEIGHTS = (4, 8)
-CTAS_PER_SM = (0, 3)
+# (tile_w, tile_h) -> 16 x 8, 16 x 16, 32 x 8 and 32 x 16 pixel tiles
+TILE_SHAPES = ((16, 4), (16, 8), (32, 4), (32, 8))
+CTAS_PER_SM = (0,)
 SPLIT = (0, 1)
-# (tile_h, ctas_per_sm, split_sweep); 2-row tiles and 2 CTAs per SM never
-# won a sweep on the room scene (fewer resident warps) and are left out
-CANDIDATES: Tuple[Tuple[int, int, int], ...] = tuple(
-    (th, c, sp) for th in TILE_HEIGHTS for c in CTAS_PER_SM for sp in SPLIT)
+# (tile_h, ctas_per_sm, split_sweep, tile_w); 2-row tiles and 1-3 CTAs per
+# SM never won a sweep on the room scene (fewer resident warps) and are left
+# out of the default list
+CANDIDATES: Tuple[Tuple[int, ...], ...] = tuple(
+    (th, c, sp, tw) for tw, th in TILE_SHAPES for c in CTAS_PER_SM for sp in SPLIT)
 
 
 def _copy_params(p: _abi.gmvs_params) -> _abi.gmvs_params:
@@ -66,6 +69,7 @@ class TuneResult:
         q = _copy_params(params)
         q.tile_h, q.ctas_per_sm = self.best[0], self.best[1]
         q.split_sweep = self.best[2] if len(self.best) > 2 else 0
+        q.tile_w = self.best[3] if len(self.best) > 3 else 0
         return q
 
 
@@ -93,7 +97,7 @@ class Autotuner:
 
     def tune(self, views: Sequence[ViewInputs], params: _abi.gmvs_params,
              stream: Optional[torch.cuda.Stream] = None) -> TuneResult:
-        """Best (tile_h, ctas_per_sm, split_sweep) for this kind of batch (cached)."""
+        """Best (tile_h, ctas_per_sm, split_sweep, tile_w) for this kind of batch (cached)."""
         key = tune_key(views, params)
         if key in self.cache:
             return self.cache[key]
@@ -105,8 +109,9 @@ class Autotuner:
         for cand in self.candidates:
             th, c = cand[0], cand[1]
             sp = cand[2] if len(cand) > 2 else 0
+            tw = cand[3] if len(cand) > 3 else 0
             p = _copy_params(params)
-            p.tile_h, p.ctas_per_sm, p.split_sweep = th, c, sp
+            p.tile_h, p.ctas_per_sm, p.split_sweep, p.tile_w = th, c, sp, tw
             plan = Plan(sample, p, ws, st)
             try:
                 plan.launch(st)  # warm-up (module load, first-touch)
@@ -116,7 +121,7 @@ class Autotuner:
                     plan.launch(st)
                 e1.record(st)
                 plan.check(st)
-                ms[f"{th},{c},{sp}"] = e0.elapsed_time(e1) / self.reps
+                ms[",".join(str(x) for x in (th, c, sp, tw)[:max(3, len(cand))])] = e0.elapsed_time(e1) / self.reps
             finally:
                 plan.close()
         best = min(ms, key=ms.get)

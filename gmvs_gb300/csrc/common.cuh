@@ -79,6 +79,7 @@ struct DevParams {
     int* nbi;
     int ca_slots;  // warp blocks in `ca`
     int nb_units;  // unit blocks in `nbc` / `nbi`
+    int wide;      // 32-pixel-wide tiles: the tile list pairs 16-column tiles (see unit_tile)
 };
 
 // A tile is TW columns x TH thread rows of one view; thread row r covers
@@ -145,6 +146,21 @@ __device__ __forceinline__ uint32_t phase_of(int pass_index, int step) {
 // footprint stays in L2; a static stride over the list lets the resident
 // CTAs drift apart across the whole batch and thrash L2 at full size.  The
 // last warp to finish resets the queue for the next launch on the stream.
+// Work unit u (one thread row of one 16-column tile) -> (tile, thread row).
+// Plain order: all TH rows of tile t, then tile t + 1.  Wide (32-pixel) tiles:
+// the tile list holds 16-column tiles in left/right pairs, and consecutive
+// units alternate between the two halves of one row, so the warps in flight
+// cover a 32 x 2*TH pixel block.
+__device__ __forceinline__ void unit_tile(int u, int TH, int wide, int& t, int& row) {
+    if (!wide) {
+        t = u / TH;
+        row = u - t * TH;
+        return;
+    }
+    const int s = u / (2 * TH), r = u - s * 2 * TH;
+    row = r >> 1;
+    t = 2 * s + (r & 1);
+}
 __device__ __forceinline__ int claim_unit(int* q, unsigned lane) {
     int u = 0;
     if (lane == 0) u = atomicAdd(q + 1, 1);

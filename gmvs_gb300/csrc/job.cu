@@ -198,6 +198,18 @@ extern "C" int32_t gmvs_job_create(gmvs_ctx* ctx, const gmvs_camera* cams, int32
             ctx->last_error = std::string(who) + ": problem " + std::to_string(k) + " is out of range";
             return fail(GMVS_ERR_INVALID, ctx->last_error);
         }
+        // caught here rather than by the fusion after every pass has run
+        for (int j = 0; j < p.num_ngb; ++j) {
+            std::string why;
+            if (p.src_image_ids[j] == p.ref_image_id) why = "a source view equals the reference view";
+            for (int i = 0; why.empty() && i < j; ++i)
+                if (p.src_image_ids[i] == p.src_image_ids[j])
+                    why = "source view " + std::to_string(p.src_image_ids[j]) + " is listed twice";
+            if (!why.empty()) {
+                ctx->last_error = std::string(who) + ": problem " + std::to_string(k) + ": " + why;
+                return fail(GMVS_ERR_INVALID, ctx->last_error);
+            }
+        }
     }
     std::vector<char> is_ref(num_images, 0);
     for (int32_t k = 0; k < num_problems; ++k)

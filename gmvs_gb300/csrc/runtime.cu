@@ -193,8 +193,16 @@ size_t bytes_per_pixel(int variant, const gmvs_params* p) {
     }
 }
 
-// a tile is 16 pixel columns (one lane pair per pixel in the PatchMatch kernels)
+// a tile is 16 pixel columns (one lane pair per pixel in the PatchMatch kernels);
+// tile_w = 32 orders the work as 32-pixel-wide blocks of two such tiles
 int tile_w_of(const gmvs_params*) { return 16; }
+bool wide_tiles(const gmvs_params* p) { return p->tile_w == 32; }
+// 16-column tiles per tile row of a view (an even count for wide tiles: the
+// right tile of the last pair may lie past the image and holds no pixel)
+int tiles_across(int width, const gmvs_params* p) {
+    const int n = (width + 15) / 16;
+    return wide_tiles(p) ? (n + 1) / 2 * 2 : n;
+}
 int tile_h_of(const gmvs_params* p) { return p->tile_h > 0 ? p->tile_h : 4; }
 
 int num_offsets(const gmvs_params* p) {
@@ -214,7 +222,8 @@ int32_t validate(const gmvs_view_pass* views, int32_t n, const gmvs_params* p) {
     if (p->init_kind < 0 || p->init_kind > 2 || p->sweep_kind < 0 || p->sweep_kind > 2)
         return fail(GMVS_ERR_INVALID, "unknown init_kind / sweep_kind");
     if (p->tile_h < 0 || p->tile_h > 8) return fail(GMVS_ERR_INVALID, "tile_h must be in [0, 8]");
-    if (p->tile_w != 0 && p->tile_w != 16) return fail(GMVS_ERR_INVALID, "tile_w must be 0 or 16");
+    if (p->tile_w != 0 && p->tile_w != 16 && p->tile_w != 32)
+        return fail(GMVS_ERR_INVALID, "tile_w must be 0, 16 or 32");
     if (p->ctas_per_sm < 0 || p->ctas_per_sm > 32) return fail(GMVS_ERR_INVALID, "ctas_per_sm must be in [0, 32]");
     if (p->split_sweep != 0 && p->split_sweep != 1) return fail(GMVS_ERR_INVALID, "split_sweep must be 0 or 1");
     if (p->tex_storage != 0 && p->tex_storage != 1) return fail(GMVS_ERR_INVALID, "tex_storage must be 0 or 1");
@@ -282,7 +291,7 @@ Layout make_layout(const gmvs_view_pass* views, int32_t n, const gmvs_params* p,
     int ntiles = 0;
     for (int v = 0; v < n; ++v) {
         const int hh = (views[v].height + 1) / 2;
-        ntiles += ((views[v].width + TW - 1) / TW) * ((hh + TH - 1) / TH);
+        ntiles += tiles_across(views[v].width, p) * ((hh + TH - 1) / TH);
     }
     L.ntiles = ntiles;
     L.tiles = off;
@@ -552,6 +561,7 @@ int32_t build_plan(gmvs_plan* P, const gmvs_view_pass* views, int32_t n, const g
     int nmax = 1;
     for (int v = 0; v < n; ++v) nmax = std::max(nmax, views[v].num_src);
     fill_params(P->dprm, p, nmax);
+    P->dprm.wide = wide_tiles(p) ? 1 : 0;
     if (with_state) {
         P->dprm.ca = (float*)(P->ws + L.ca);
         P->dprm.ca_slots = num_sms() * L.ca_ctas * tile_h_of(p);
@@ -595,8 +605,9 @@ int32_t build_plan(gmvs_plan* P, const gmvs_view_pass* views, int32_t n, const g
             hv[v].fin = (float4*)b;
         }
         const int hh = (views[v].height + 1) / 2;
+        const int across = tiles_across(views[v].width, p);
         for (int y = 0; y < hh; y += TH)
-            for (int x = 0; x < views[v].width; x += TW) ht.push_back(Tile{v, x, y, -1});
+            for (int k = 0; k < across; ++k) ht.push_back(Tile{v, k * TW, y, -1});
     }
     int hdr[4] = {0, L.ntiles, 0, 0};  // error word, tile queue (count, next unit, warps done)
     cudaError_t e = cudaMemcpyAsync(P->ws, hdr, sizeof(hdr), cudaMemcpyHostToDevice, st);

@@ -78,17 +78,19 @@ def _unfilter(data: bytes, h: int, w: int, bpp: int) -> np.ndarray:
     return out
 
 
-def read_png(path: str) -> np.ndarray:
+def _read_png(path: str):
+    """(pixels, set of chunk tags) of an 8-bit PNG."""
     with open(path, "rb") as f:
         blob = f.read()
     if blob[:8] != _SIG:
         raise ValueError(f"{path} is not a PNG")
-    pos, idat, hdr = 8, [], None
+    pos, idat, hdr, tags = 8, [], None, set()
     while pos < len(blob):
         (n,) = struct.unpack(">I", blob[pos:pos + 4])
         tag = blob[pos + 4:pos + 8]
         data = blob[pos + 8:pos + 8 + n]
         pos += 12 + n
+        tags.add(tag)
         if tag == b"IHDR":
             hdr = struct.unpack(">IIBBBBB", data)
         elif tag == b"IDAT":
@@ -100,27 +102,57 @@ def read_png(path: str) -> np.ndarray:
         raise ValueError("only 8-bit non-interlaced gray/RGB(A) PNGs are supported")
     ch = {0: 1, 2: 3, 4: 2, 6: 4}[ctype]
     px = _unfilter(zlib.decompress(b"".join(idat)), h, w, ch).reshape(h, w, ch)
-    return px[..., 0] if ch == 1 else px
+    return (px[..., 0] if ch == 1 else px), tags
+
+
+def read_png(path: str) -> np.ndarray:
+    return _read_png(path)[0]
+
+
+# libpng's RGB -> gray weights as OpenCV's PNG decoder requests them for
+# IMREAD_GRAYSCALE (png_set_rgb_to_gray(png, 1, 0.299, 0.587)): the 1e-5 fixed
+# point values 29900 and 58700 scaled to 1/32768 with truncation, blue the rest.
+PNG_GRAY_RED, PNG_GRAY_GREEN = 29900 * 32768 // 100000, 58700 * 32768 // 100000  # 9797, 19234
+PNG_GRAY_BLUE = 32768 - PNG_GRAY_RED - PNG_GRAY_GREEN  # 3737
+
+
+def png_rgb_to_gray(r: np.ndarray, g: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """libpng's 8-bit RGB -> gray step without gamma correction
+    (png_do_rgb_to_gray): the weighted sum shifted right by 15, truncated;
+    equal channels come through unchanged (the sum gives the same value)."""
+    acc = (PNG_GRAY_RED * r.astype(np.int64) + PNG_GRAY_GREEN * g.astype(np.int64) +
+           PNG_GRAY_BLUE * b.astype(np.int64))
+    return (acc >> 15).astype(np.uint8)
 
 
 def imread_gray(path: str) -> np.ndarray:
-    """uint8 [H, W] like cv2.imread(path, cv2.IMREAD_GRAYSCALE)."""
+    """uint8 [H, W] like cv2.imread(path, cv2.IMREAD_GRAYSCALE).
+
+    PNG content is decoded here.  A colour PNG is reduced to gray with
+    libpng's integer transform (png_rgb_to_gray), which is what OpenCV's PNG
+    decoder asks libpng for; that holds for files without colour-space
+    chunks, where libpng applies no gamma correction.  A colour PNG with a
+    gAMA, sRGB or iCCP chunk would go through libpng's gamma tables, which
+    this reader does not restate: cv2 decodes it when importable, otherwise
+    the call fails.  (Neither OpenCV nor libpng is present to pin the
+    transform against; gray PNGs, the synthetic scenes' format, need none.)
+    """
     with open(path, "rb") as f:
         is_png = f.read(8) == _SIG
-    if not is_png:
-        try:
-            import cv2  # noqa: F401
-        except ImportError as e:
-            raise RuntimeError(f"{path}: only PNG content can be read without OpenCV") from e
+    if is_png:
+        px, tags = _read_png(path)
+        if px.ndim == 2:
+            return px
+        if px.shape[2] == 2:  # gray + alpha: the alpha is stripped
+            return np.ascontiguousarray(px[..., 0])
+        if not tags & {b"gAMA", b"sRGB", b"iCCP"}:
+            return png_rgb_to_gray(px[..., 0], px[..., 1], px[..., 2])
+    try:
         import cv2
-
-        img = cv2.imread(path, cv2.IMREAD_GRAYSCALE)
-        if img is None:
-            raise RuntimeError(f"cannot read {path}")
-        return img
-    px = read_png(path)
-    if px.ndim == 2:
-        return px
-    rgb = px[..., :3].astype(np.float64)
-    # ITU-R BT.601 luma, rounded, the conversion cv2 uses for RGB -> gray
-    return np.clip(np.rint(0.299 * rgb[..., 0] + 0.587 * rgb[..., 1] + 0.114 * rgb[..., 2]), 0, 255).astype(np.uint8)
+    except ImportError as e:
+        what = "colour PNGs with colour-space chunks" if is_png else "non-PNG content"
+        raise RuntimeError(f"{path}: {what} can only be read with OpenCV") from e
+    img = cv2.imread(path, cv2.IMREAD_GRAYSCALE)
+    if img is None:
+        raise RuntimeError(f"cannot read {path}")
+    return img

@@ -55,12 +55,20 @@ class ScenePipeline:
 
     def __init__(self, scene: SceneInputs, geom_iters: int = 2, geom_consistent: int = 3, mode: str = "batched",
                  staging: int = _abi.STAGE_AUTO, tile_h: int = 0, prior_threads: int = 8, params=None,
-                 graphs: bool = False, autotuner=None, overlap: bool = True):
+                 graphs: bool = False, autotuner=None, overlap: bool = True, mirror_streams: bool = False):
         if mode not in ("batched", "plain"):
             raise ValueError("mode is 'batched' or 'plain'")
         if graphs and mode != "batched":
             raise ValueError("CUDA graphs replay the batched launch chains")
         self.graphs = graphs
+        # mirror_streams: the random streams that the module mirrors
+        # (planar_initer.PlanarInit, src.PatchMatcher) use, so that the
+        # reference's own call sequence over them gives this pipeline's maps:
+        # one stream shared by every view in the random and prior passes (the
+        # reference seeds every view alike, curand_init(3407, y, x),
+        # patch_match_kernel.cu:1491) and one pass index for every geometric
+        # pass.  By default each view and pass draws its own stream.
+        self.mirror_streams = mirror_streams
         self._graphs: Dict[str, torch.cuda.CUDAGraph] = {}
         if autotuner is not None and mode != "batched":
             raise ValueError("the autotuner picks launch shapes of the batched launch chains")
@@ -112,8 +120,9 @@ class ScenePipeline:
         for ref, src in problems:
             ids = [ref] + list(src)
             dmin, dmax = _range(sc.cams[ref])
+            sid = 0 if self.mirror_streams and kind != "geom" else ref
             v = ViewInputs(cams=[sc.cams[i] for i in ids], images=[sc.images[i] for i in ids], depth_min=dmin,
-                           depth_max=dmax, stream_id=ref)
+                           depth_max=dmax, stream_id=sid)
             if kind == "prior":
                 v.prior_planes = self.prior_planes[ref]
                 v.prior_masks = self.prior_masks[ref]
@@ -155,7 +164,7 @@ class ScenePipeline:
         out += [(f"prior{g}" if multi else "prior", "prior", 1, 0, 1, grp) for g, grp in enumerate(self.groups)]
         buf = 1
         for g in range(self.geom_iters):
-            out.append((f"geom{g}", "geom", 1 - buf, buf, 2 + g, None))
+            out.append((f"geom{g}", "geom", 1 - buf, buf, 2 if self.mirror_streams else 2 + g, None))
             buf = 1 - buf
         return out
 

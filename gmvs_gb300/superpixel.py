@@ -39,9 +39,12 @@ def default_params(**overrides) -> gmvs_superpixel_params:
 
 
 def bgr_to_gray(image: np.ndarray) -> np.ndarray:
-    """ITU-R BT.601 luma of a BGR uint8 image, rounded to nearest."""
-    x = image.astype(np.float64)  # summed in imageio.imread_gray's order: R, G, B
-    return np.clip(np.rint(0.299 * x[..., 2] + 0.587 * x[..., 1] + 0.114 * x[..., 0]), 0, 255).astype(np.uint8)
+    """The gray image cv2.imread(path, IMREAD_GRAYSCALE) gives for a colour
+    PNG whose cv2.imread(path) is `image` (BGR uint8): libpng's integer
+    transform, as imageio.imread_gray applies it."""
+    from .imageio import png_rgb_to_gray
+
+    return png_rgb_to_gray(image[..., 2], image[..., 1], image[..., 0])
 
 
 def _device_u8(a, shape, name: str, dev: torch.device) -> torch.Tensor:

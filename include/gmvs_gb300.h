@@ -112,7 +112,9 @@ typedef struct gmvs_params {
     int32_t sampler;          /* gmvs_sampler */
     int32_t staging;          /* gmvs_staging */
     int32_t pass_index;       /* decorrelates the Philox streams of successive passes */
-    int32_t tile_w;           /* sweep tile width in pixels: 0 or 16 (one lane pair per pixel) */
+    int32_t tile_w;           /* sweep tile width in pixels: 0 or 16 (one lane pair per pixel), or 32:
+                                 the warps in flight take 32-pixel-wide blocks of two 16-column tiles,
+                                 row by row (same results; another memory-access order) */
     int32_t tile_h;           /* sweep tile height in thread rows, 1..8 (0 = 4); a tile is 16 x 2*tile_h pixels */
     int32_t run_filter;       /* 1 = depth/normal conversion + checkerboard median filter */
     int32_t ctas_per_sm;      /* PatchMatch kernels: resident CTAs per SM (0 = as many as fit); fewer CTAs
@@ -236,9 +238,11 @@ GMVS_API int32_t gmvs_fuse(const gmvs_fuse_view* args, void* scratch, size_t scr
  * could fail.  Same inputs, outputs and results as gmvs_fuse; the per-pixel
  * scratch is a library-owned device array of GMVS_FUSE_FIXED_MAX_PIXELS
  * int32 entries (16 MiB), and views with height * width above that are
- * rejected with GMVS_ERR_INVALID.  The first call on each device (the
- * device current at the call) looks the array up, which may load a module:
- * make that first call before any stream capture.  Every call re-initialises
+ * rejected with GMVS_ERR_INVALID.  The first call in each CUDA context
+ * (normally: on each device, in the device's primary context) looks the
+ * array up, which may load a module: make that first call before any stream
+ * capture.  A new context on the device (after cudaDeviceReset, or another
+ * context made current through the driver API) is looked up afresh.  Every call re-initialises
  * the part of the array it uses on `stream`, so nothing has to be cleared
  * beforehand; but all calls on a device share the one array, so calls whose
  * work can overlap on the device (different streams, several host threads)

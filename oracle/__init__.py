@@ -24,7 +24,7 @@ class oracle_params(ctypes.Structure):
     _fields_ = [("max_iterations", _i), ("patch_size", _i), ("radius_increment", _i), ("sigma_spatial", _f),
                 ("sigma_color", _f), ("top_k", _i), ("depth_min", _f), ("depth_max", _f), ("init_kind", _i),
                 ("sweep_kind", _i), ("sampler", _i), ("run_filter", _i), ("seed", ctypes.c_uint64),
-                ("pass_index", _i), ("stream_id", _i)]
+                ("pass_index", _i), ("stream_id", _i), ("fp64", _i), ("max_half_sweeps", _i)]
 
 
 class OCamera(ctypes.Structure):
@@ -123,8 +123,10 @@ def u01(x: int) -> float:
 
 
 def ncc_costs(cam_args, images: np.ndarray, planes: np.ndarray, params: oracle_params, fp64: bool = False,
-              nthreads: int = 0):
+              nthreads: int = 0, ref_chain: bool = False):
     """images: float32 [1+N, H, W]; planes: float32 [H, W, 4] camera frame.
+    fp64: the FP64 oracle; ref_chain: the reference's own fp32 operation
+    chain instead of the shared formulation.
     Returns (costs [N, H, W], init_cost [H, W], init_views [H, W] uint32)."""
     imgs = np.ascontiguousarray(images, np.float32)
     n1, H, W = imgs.shape
@@ -134,7 +136,7 @@ def ncc_costs(cam_args, images: np.ndarray, planes: np.ndarray, params: oracle_p
     iv = np.zeros((H, W), np.uint32)
     cams = cameras(cam_args)
     rc = lib().oracle_ncc_costs(cams, n1 - 1, H, W, _np_ptr(imgs), ctypes.byref(params), _np_ptr(pl),
-                                _np_ptr(costs), _np_ptr(ic), _np_ptr(iv), int(fp64), nthreads)
+                                _np_ptr(costs), _np_ptr(ic), _np_ptr(iv), 2 if ref_chain else int(fp64), nthreads)
     if rc != 0:
         raise RuntimeError(f"oracle_ncc_costs failed ({rc})")
     return costs, ic, iv

@@ -84,6 +84,8 @@ struct oracle_params {
     uint64_t seed;
     int32_t pass_index;
     int32_t stream_id;
+    int32_t fp64;             // 1: every NCC of the pass in double precision (the FP64 CPU baseline)
+    int32_t max_half_sweeps;  // > 0: stop after this many half-sweeps (0: 2 * max_iterations)
 };
 
 }  // extern "C"
@@ -437,6 +439,7 @@ struct ViewSet {
     float sigma_spatial, sigma_color;
     int top_k;
     std::vector<ViewConst> vc;  // per source view
+    int fp64 = 0;               // NCCs in double precision (bilateral_ncc<double>)
     void init_consts() {
         vc.clear();
         for (int j = 1; j <= N; ++j) vc.push_back(view_consts(cams[0], cams[j]));
@@ -611,9 +614,14 @@ inline float ncc_f32(const ViewSet& vs, int src, int px, int py, const F4& pl) {
     return std::fmax(0.0f, std::fmin(2.0f, 1.0f - cov / vrs));
 }
 
+// One NCC of a pass: the shared fp32 formulation, or FP64 for the baseline.
+inline float ncc_eval(const ViewSet& vs, int src, int px, int py, const F4& pl) {
+    return vs.fp64 ? (float)bilateral_ncc<double>(vs, src, px, py, pl) : ncc_f32(vs, src, px, py, pl);
+}
+
 // ComputeMultiViewCostVector (patch_match_kernel.cu:571-588)
 inline void cost_vector(const ViewSet& vs, int px, int py, const F4& pl, float* out) {
-    for (int i = 1; i <= vs.N; ++i) out[i - 1] = ncc_f32(vs, i, px, py, pl);
+    for (int i = 1; i <= vs.N; ++i) out[i - 1] = ncc_eval(vs, i, px, py, pl);
 }
 
 // ComputeMultiViewInitialCostandSelectedViews (patch_match_kernel.cu:518-569)
@@ -1129,7 +1137,7 @@ void sweep_pixel(const PassCtx& ctx, int px, int py, int iter, int colour, float
             float cvk[kMaxNgb];
             for (int j = 0; j < N; ++j) cvk[j] = 0.0f;
             for (int j = 0; j < N; ++j)
-                if (view_weights[j] > 0) cvk[j] = ncc_f32(vs, j + 1, px, py, cand);
+                if (view_weights[j] > 0) cvk[j] = ncc_eval(vs, j + 1, px, py, cand);
             float tc = 0.0f;
             for (int j = 0; j < N; ++j) {
                 if (view_weights[j] > 0) {
@@ -1223,8 +1231,11 @@ float oracle_pm_cosf(float x) { return pmath::cosf_(x); }
 float oracle_pm_acosf(float x) { return pmath::acosf_(x); }
 
 // Per-view NCC costs of given camera-frame planes (float4 per pixel) and the
-// initial multi-view cost / selected views.  fp64 != 0 evaluates the NCC in
-// double precision (the FP64 oracle).
+// initial multi-view cost / selected views.  fp64 = 1 evaluates the NCC in
+// double precision (the FP64 oracle); fp64 = 2 in the reference's own fp32
+// chain (ComputeHomography / ComputeCorrespondingPoint / ComputeBilateralNCC
+// in float, in the reference's operation order, without fused multiply-adds
+// and with IEEE exp, division and square root).
 int oracle_ncc_costs(const Cam* cams, int num_src, int H, int W, const float* images, const oracle_params* prm,
                      const float* planes, float* costs, float* init_cost, uint32_t* init_views, int fp64,
                      int nthreads) {
@@ -1240,8 +1251,10 @@ int oracle_ncc_costs(const Cam* cams, int num_src, int H, int W, const float* im
             const int c = y * W + x;
             float cv[kMaxNgb];
             for (int s = 1; s <= num_src; ++s) {
-                if (fp64)
+                if (fp64 == 1)
                     cv[s - 1] = (float)bilateral_ncc<double>(vs, s, x, y, pl[c]);
+                else if (fp64 == 2)
+                    cv[s - 1] = bilateral_ncc<float>(vs, s, x, y, pl[c]);
                 else
                     cv[s - 1] = ncc_f32(vs, s, x, y, pl[c]);
                 if (costs) costs[(size_t)(s - 1) * H * W + c] = cv[s - 1];
@@ -1274,6 +1287,7 @@ int oracle_run_pass(const Cam* cams, int num_src, int H, int W, const float* ima
     ctx.vs = ViewSet{H, W, num_src, cams, images, depths, prm->sampler, prm->patch_size, prm->radius_increment,
                      prm->sigma_spatial, prm->sigma_color, prm->top_k, {}};
     ctx.vs.init_consts();
+    ctx.vs.fp64 = prm->fp64;
     ctx.prm = *prm;
     ctx.prior_planes = reinterpret_cast<const F4*>(prior_planes);
     ctx.prior_masks = prior_masks;
@@ -1285,10 +1299,12 @@ int oracle_run_pass(const Cam* cams, int num_src, int H, int W, const float* ima
     for (int y = 0; y < H; ++y)
         for (int x = 0; x < W; ++x) init_pixel(ctx, x, y, depths, ref_normal, ip, init_costs, a);
 
+    int half_sweeps = 0;
     for (int it = 0; it < prm->max_iterations; ++it) {
         // cost_threshold = 0.8 * expf(iter*iter / -90) (patch_match_kernel.cu:1143)
         const float thr = (float)(0.8 * (double)pmath::expf_((float)(it * it) / (-90.0f)));
         for (int colour = 0; colour < 2; ++colour) {
+            if (prm->max_half_sweeps > 0 && half_sweeps++ >= prm->max_half_sweeps) break;
             b = a;
 #pragma omp parallel for schedule(dynamic, 2) num_threads(nt)
             for (int y = 0; y < H; ++y)

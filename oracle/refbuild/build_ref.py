@@ -1,11 +1,32 @@
-"""Compile the reference's own module-B kernels (gmvs/src/patch_match.cu and
-gmvs/src/fusion.cu, read where they lie under /root/reference) to cubins for
-sm_103a, written to oracle/_ref/.  Test infrastructure only: the cubins are
-launched by oracle/refbuild/ref_harness.py to produce golden vectors.
+"""Compile the reference's own GPU kernels to cubins for sm_103a, written to
+oracle/_ref/.  Test and measurement infrastructure only: the cubins are
+launched by oracle/refbuild/ref_harness.py to produce golden vectors and to
+time the reference's plain per-view GPU path.
 
-The only change to the reference build is an include shim for
-cuda_texture_types.h, which CUDA 13 no longer ships.  Module A
-(gmvs/lib/src/*) needs OpenCV and is not buildable here.
+  ref_patch_match.cubin  gmvs/src/patch_match.cu      (module B, geometric pass)
+  ref_fusion.cubin       gmvs/src/fusion.cu           (module B, fusion)
+  ref_planar.cubin       gmvs/lib/src/patch_match_kernel.cu
+                                                      (module A, random and
+                                                       planar-prior passes)
+  ref_planar_ieee.cubin, ref_patch_match_ieee.cubin, ref_fusion_ieee.cubin
+                         the same sources without fast math and without
+                         fused multiply-adds (-fmad=false): the reference's
+                         own operation chains in IEEE fp32, against which
+                         the oracle's restatements of those chains are pinned
+
+The sources are read where they lie in the reference checkout: the folder
+named by GMVS_REFERENCE, or else a `reference` folder beside this
+repository's root.  The flags are the reference's own: module B as torch's
+CUDAExtension builds it (no fast math), module A as its CMakeLists.txt
+(-O3 --use_fast_math --maxrregcount=128), retargeted to sm_103a.
+
+Two include shims stand in for headers this toolchain lacks
+(oracle/refbuild/shim): cuda_texture_types.h, which CUDA 13 no longer ships,
+and a declaration-only set of opencv2 headers.  Module A's header declares
+cv::Mat, cv::Point, cv::Rect, cv::Mat_ and cv::Vec3b in PlanarInit's members
+and signatures, but neither the kernels nor the launcher in
+patch_match_kernel.cu touch an OpenCV object, so empty types suffice and no
+OpenCV code is compiled.
 """
 
 import os
@@ -15,40 +36,64 @@ import sysconfig
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
-REF = os.environ.get("GMVS_REFERENCE", "/root/reference")
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = os.environ.get("GMVS_REFERENCE") or os.path.join(os.path.dirname(REPO), "reference")
+
+# (cubin name, source under the checkout, include folders under the checkout, extra flags)
+UNITS = [
+    ("patch_match", "gmvs/src/patch_match.cu", ["gmvs/include"],
+     ["-DTORCH_EXTENSION_NAME=gmvs_src_ref", "-D__CUDA_NO_HALF_OPERATORS__"]),
+    ("fusion", "gmvs/src/fusion.cu", ["gmvs/include"],
+     ["-DTORCH_EXTENSION_NAME=gmvs_src_ref", "-D__CUDA_NO_HALF_OPERATORS__"]),
+    ("planar", "gmvs/lib/src/patch_match_kernel.cu", ["gmvs/lib/include"],
+     ["--use_fast_math", "--maxrregcount=128"]),
+    ("planar_ieee", "gmvs/lib/src/patch_match_kernel.cu", ["gmvs/lib/include"],
+     ["--maxrregcount=128", "-fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
+    ("patch_match_ieee", "gmvs/src/patch_match.cu", ["gmvs/include"],
+     ["-DTORCH_EXTENSION_NAME=gmvs_src_ref", "-D__CUDA_NO_HALF_OPERATORS__", "-fmad=false"]),
+    ("fusion_ieee", "gmvs/src/fusion.cu", ["gmvs/include"],
+     ["-DTORCH_EXTENSION_NAME=gmvs_src_ref", "-D__CUDA_NO_HALF_OPERATORS__", "-fmad=false"]),
+]
 
 
 def available() -> bool:
     """True where the reference sources are present (not on the GPU machine)."""
-    return os.path.isdir(os.path.join(REF, "gmvs", "src"))
+    return all(os.path.isfile(os.path.join(REF, src)) for _, src, _, _ in UNITS)
+
+
+def cubin(name: str) -> str:
+    return os.path.join(OUT, f"ref_{name}.cubin")
+
+
+def _torch_includes() -> list:
+    import torch.utils.cpp_extension as ce
+
+    return ce.include_paths() + [sysconfig.get_paths()["include"]]
 
 
 def build(force: bool = False) -> list:
-    import torch.utils.cpp_extension as ce
-
     if not available():
-        raise RuntimeError(f"reference sources not found under {REF}")
+        raise RuntimeError(f"reference sources not found under {REF} (set GMVS_REFERENCE)")
     os.makedirs(OUT, exist_ok=True)
-    srcs = [os.path.join(REF, "gmvs", "src", f"{n}.cu") for n in ("patch_match", "fusion")]
-    outs = [os.path.join(OUT, f"ref_{n}.cubin") for n in ("patch_match", "fusion")]
-    if not force and all(os.path.exists(o) for o in outs) and \
-            min(os.path.getmtime(o) for o in outs) > max(os.path.getmtime(s) for s in srcs):
-        return outs
-    incs = [os.path.join(HERE, "shim"), os.path.join(REF, "gmvs", "include")] + ce.include_paths() + \
-        [sysconfig.get_paths()["include"]]
-    outs = []
-    for name in ("patch_match", "fusion"):
-        out = os.path.join(OUT, f"ref_{name}.cubin")
-        cmd = ["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
-               "-DTORCH_EXTENSION_NAME=gmvs_src_ref", "-D__CUDA_NO_HALF_OPERATORS__",
-               *[f"-I{i}" for i in incs], os.path.join(REF, "gmvs", "src", f"{name}.cu"), "-o", out]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"nvcc failed for {name}.cu:\n{r.stderr[-4000:]}")
-        outs.append(out)
-    return outs
+    jobs = []
+    for name, src, incs, flags in UNITS:
+        path = os.path.join(REF, src)
+        out = cubin(name)
+        if not force and os.path.exists(out) and os.path.getmtime(out) > os.path.getmtime(path):
+            continue
+        inc = [os.path.join(HERE, "shim")] + [os.path.join(REF, i) for i in incs]
+        if not name.startswith("planar"):
+            inc += _torch_includes()
+        cmd = ["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", *flags,
+               "-diag-suppress", "550,177", *[f"-I{i}" for i in inc], path, "-o", out]
+        jobs.append((name, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)))
+    for name, proc in jobs:
+        _, err = proc.communicate()
+        if proc.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {name}:\n{err[-4000:]}")
+    return [cubin(n) for n, _, _, _ in UNITS]
 
 
 if __name__ == "__main__":
-    print("\n".join(build()))
+    print("\n".join(build(force="--force" in sys.argv)))
     sys.exit(0)

@@ -9,10 +9,12 @@ import pytest
 from gmvs_gb300 import _abi, autotune
 
 
-def test_candidates_cover_tile_shapes_residency_and_split():
-    assert {c[0] for c in autotune.CANDIDATES} == {4, 8}  # 16x8 and 16x16 pixel tiles
-    assert {c[1] for c in autotune.CANDIDATES} == {0, 3}
+def test_candidates_cover_tile_shapes_and_split():
+    # 16x8, 16x16, 32x8 and 32x16 pixel tiles, single and split half-sweeps
+    assert {(c[3], 2 * c[0]) for c in autotune.CANDIDATES} == {(16, 8), (16, 16), (32, 8), (32, 16)}
     assert {c[2] for c in autotune.CANDIDATES} == {0, 1}
+    p = autotune.TuneResult("k", (4, 0, 1, 32)).apply(_abi.default_params())
+    assert (p.tile_h, p.ctas_per_sm, p.split_sweep, p.tile_w) == (4, 0, 1, 32)
 
 
 def test_cache_file_round_trip(tmp_path, gmvs_lib):
@@ -36,20 +38,20 @@ def test_launch_shape_does_not_change_results(gmvs_lib, small, cuda):
     ids = [ref] + list(src)
     outs = {}
     for sampler, staging in ((_abi.SAMPLER_TEX, _abi.STAGE_AUTO), (_abi.SAMPLER_CLAMP, _abi.STAGE_QUAD_F16)):
-        for th, c in ((4, 0), (2, 3), (8, 2), (1, 1)):
+        for th, c, tw in ((4, 0, 0), (2, 3, 0), (8, 2, 0), (1, 1, 0), (4, 0, 32), (8, 0, 32)):
             v = gpu_view(small, ids, cuda, 0.3, 6.0)
             v.allocate_outputs(with_planes=True)
             p = engine.params_struct(sampler=sampler, staging=staging, tile_h=th, ctas_per_sm=c,
-                                     split_sweep=int(th == 8))
+                                     split_sweep=int(th == 8), tile_w=tw)
             engine.run_passes([v], p, engine.Workspace())
-            outs[(sampler, th, c)] = (v.out_depth.cpu().numpy(), v.out_cost.cpu().numpy(),
-                                      v.out_planes.cpu().numpy())
-        base = outs[(sampler, 4, 0)]
-        for (s, th, c), o in outs.items():
+            outs[(sampler, th, c, tw)] = (v.out_depth.cpu().numpy(), v.out_cost.cpu().numpy(),
+                                          v.out_planes.cpu().numpy())
+        base = outs[(sampler, 4, 0, 0)]
+        for (s, th, c, tw), o in outs.items():
             if s != sampler:
                 continue
             for a, b in zip(o, base):
-                assert np.array_equal(a, b, equal_nan=True), (sampler, th, c)
+                assert np.array_equal(a, b, equal_nan=True), (sampler, th, c, tw)
 
 
 @pytest.mark.gpu

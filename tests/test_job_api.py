@@ -100,3 +100,28 @@ def test_job_api_equals_python_pipeline(gmvs_lib, cuda):
     finally:
         L.gmvs_job_destroy(job)
         L.gmvs_ctx_destroy(ctx)
+
+
+@pytest.mark.gpu
+def test_job_api_rejects_bad_problems(gmvs_lib, cuda):
+    """A source view equal to its reference view, or listed twice, is refused
+    at gmvs_job_create, before any pass runs (the fusion would refuse the
+    first only at the end)."""
+    from gmvs_gb300 import engine
+
+    L = _abi.lib()
+    ctx, job = ctypes.c_void_p(), ctypes.c_void_p()
+    assert L.gmvs_ctx_create(0, ctypes.byref(ctx)) == 0
+    try:
+        cams = (_abi.gmvs_camera * 3)()
+        for c in cams:
+            c.height, c.width = 8, 8
+        for src, why in (([1, 0], "equals the reference view"), ([1, 2, 1], "listed twice")):
+            probs = (_abi.gmvs_problem * 1)(engine.make_problem(0, src))
+            rc = L.gmvs_job_create(ctx, cams, 3, 8, 8, 1 << 20, None, probs, 1, ctypes.byref(job))
+            assert rc == _abi.ERR_INVALID and not job.value
+            buf = ctypes.create_string_buffer(512)
+            L.gmvs_ctx_last_error(ctx, buf, 512)
+            assert why in buf.value.decode(), buf.value
+    finally:
+        L.gmvs_ctx_destroy(ctx)

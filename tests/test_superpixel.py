@@ -247,7 +247,7 @@ def test_superpixels_rejects_bad_arguments_before_any_device_work(gmvs_lib):
 
 def test_read_bgr_and_gray_conversion(tmp_path):
     """cv2.imread's BGR order and gray images read back as three equal
-    channels; the gray conversion is BT.601 rounded, as imread_gray."""
+    channels; the gray conversion is libpng's, as imread_gray."""
     from gmvs_gb300 import superpixel as sp
     from gmvs_gb300.imageio import imread_gray, write_png
 
@@ -262,6 +262,21 @@ def test_read_bgr_and_gray_conversion(tmp_path):
     q = os.path.join(tmp_path, "g.png")
     write_png(q, g)
     assert np.array_equal(sp.read_bgr(q), np.repeat(g[..., None], 3, axis=2))
+
+
+def test_png_gray_transform():
+    """libpng's 8-bit RGB -> gray weights (1/32768: 9797, 19234, 3737) and its
+    truncating shift, checked by hand on a few triples; equal channels pass
+    through unchanged; a colour PNG with a gAMA chunk needs OpenCV."""
+    from gmvs_gb300.imageio import PNG_GRAY_BLUE, PNG_GRAY_GREEN, PNG_GRAY_RED, png_rgb_to_gray
+
+    assert (PNG_GRAY_RED, PNG_GRAY_GREEN, PNG_GRAY_BLUE) == (9797, 19234, 3737)
+    rgb = np.array([[255, 0, 0], [0, 255, 0], [0, 0, 255], [10, 200, 30], [255, 255, 254]], np.uint8)
+    want = [(9797 * 255) >> 15, (19234 * 255) >> 15, (3737 * 255) >> 15,
+            (9797 * 10 + 19234 * 200 + 3737 * 30) >> 15, (9797 * 255 + 19234 * 255 + 3737 * 254) >> 15]
+    assert png_rgb_to_gray(rgb[:, 0], rgb[:, 1], rgb[:, 2]).tolist() == want == [76, 149, 29, 123, 254]
+    v = np.arange(256, dtype=np.uint8)
+    assert np.array_equal(png_rgb_to_gray(v, v, v), v)
 
 
 def test_extract_superpixel_rejects_weights():

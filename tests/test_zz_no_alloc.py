@@ -74,6 +74,44 @@ def test_fixed_scratch_matches_caller_scratch(gmvs_lib, small, cuda):
     assert fused > 0 and masks_ref.any()
 
 
+@pytest.mark.gpu
+def test_fixed_scratch_at_its_limit_then_smaller(gmvs_lib, small, cuda):
+    """A view of exactly GMVS_FUSE_FIXED_MAX_PIXELS (2048 x 2048) fills the
+    whole array; a smaller view afterwards finds a stale tail beyond its own
+    pixels, which it never reads.  Both equal gmvs_fuse with caller scratch."""
+    import torch
+
+    L = _abi.lib()
+    big = synthetic.small_scene(3, H=2048, W=2048, device=cuda)
+    assert big.hw[0] * big.hw[1] == _abi.FUSE_FIXED_MAX_PIXELS
+    stream = _abi.stream_ptr()
+    for sc, (ref, src) in ((big, big.problems[0]), (small, small.problems[3])):
+        d_in, n_in = _noisy_inputs(sc, seed=8)
+        V = sc.num_views
+        H, W = sc.hw
+        dev_d = torch.from_numpy(d_in).to(cuda)
+        dev_n = torch.from_numpy(n_in).to(cuda)
+        scratch = torch.empty(L.gmvs_fuse_scratch_bytes(H, W), dtype=torch.uint8, device=cuda)
+        outs, all_masks = [], []
+        for fixed in (False, True):
+            masks = torch.zeros((V, H, W), dtype=torch.bool, device=cuda)
+            od = torch.full((H, W), 7.0, device=cuda)
+            on = torch.full((H, W, 3), 7.0, device=cuda)
+            oc = torch.full((H, W), 7, dtype=torch.int32, device=cuda)
+            a = _fuse_args(sc, ref, src, dev_d, dev_n, masks, od, on, oc)
+            if fixed:
+                rc = L.gmvs_fuse_fixed_scratch(ctypes.byref(a), stream)
+            else:
+                rc = L.gmvs_fuse(ctypes.byref(a), scratch.data_ptr(), scratch.numel(), stream)
+            _abi.check(rc)
+            outs.append((od.cpu().numpy(), on.cpu().numpy(), oc.cpu().numpy()))
+            all_masks.append(masks)
+        (rd, rn, rcnt), (fd, fn, fcnt) = outs
+        assert np.array_equal(fcnt, rcnt) and np.array_equal(fd, rd) and np.array_equal(fn, rn)
+        assert torch.equal(all_masks[0], all_masks[1])
+        assert int((rcnt >= 3).sum()) > 0
+
+
 def test_fixed_scratch_rejects_oversized_views(gmvs_lib):
     # the size check comes before any CUDA call, so this runs without a GPU
     a = _abi.gmvs_fuse_view()
