@@ -306,13 +306,20 @@ def precision_run(sc, dev, pipe, plain_fused) -> dict:
                                  planes, oracle.make_params(sampler=0), fp64=True)
     err = np.abs(c16 - c64)
     pick = rng.random((H, W)) < 0.01
-    out = {"ncc_vs_fp64": {"sample_1pct": {"max": float(err[:, pick].max()), "mean": float(err[:, pick].mean()),
-                                           "pixels": int(pick.sum()), "sources": len(src)},
-                           "whole_view": {"max": float(err.max()), "mean": float(err.mean()),
-                                          "frac_within_1e-3": float(np.mean(err <= 1e-3)),
-                                          "frac_within_1e-4": float(np.mean(err <= 1e-4))},
+
+    def stats(e):
+        return {"max": float(e.max()), "mean": float(e.mean()), "frac_within_1e-3": float(np.mean(e <= 1e-3)),
+                "frac_within_1e-4": float(np.mean(e <= 1e-4)), "evaluations": int(e.size)}
+
+    is_gt = np.all(planes == gt.astype(np.float32), -1)
+    out = {"ncc_vs_fp64": {"sample_1pct": stats(err[:, pick]),
+                           "whole_view": stats(err),
+                           "ground_truth_hypotheses": stats(err[:, is_gt]),
+                           "random_hypotheses": stats(err[:, ~is_gt]),
                            "staging": "fp16 texel quads, fp32 moments, FP64 homography constants",
-                           "hypotheses": "room view 0, half ground truth, half random"}}
+                           "hypotheses": "room view 0 with its 10 sources, half ground truth, half random",
+                           "note": "the large errors are random planes whose fp32 homography is ill-conditioned "
+                                   "(the sample coordinates themselves move) and windows at the 1e-5 variance floor"}}
     if plain_fused is not None:
         bd, bn = pipe.fused_depth, pipe.fused_normal
         pd, pn = plain_fused

@@ -62,6 +62,8 @@ with its 10 sources; per-pixel arrays as 8 crops of 96x96, see ROOM_CROPS):
                                    the fused depth, the fused-pixel count and
                                    SHA-256 digests of the fused-pixel map and
                                    of the source masks
+  room_ieee_fuse_*                 the same from module B's fusion built
+                                   without fused multiply-adds
   room_images_sha                  digest of the rendered images (input check)
 
 Usage (on a machine with a GPU and the cubins):
@@ -329,6 +331,12 @@ def make_room(drv, rh, out_dir):
     out["room_fuse_sha"] = sha(fd > 0)
     out["room_fuse_masks_sha"] = sha(masks[ids].astype(bool))
     out["room_fuse_masks_count"] = masks[ids].reshape(len(ids), -1).sum(1).astype(np.int64)
+    outs, masks = rh.run_fusion(drv, cams, [(ref, src)], noisy_d, noisy_n, 3, module="fusion_ieee")
+    fd = outs[0][0]
+    out["room_ieee_fuse_count"] = np.int64((fd > 0).sum())
+    out["room_ieee_fuse_sha"] = sha(fd > 0)
+    out["room_ieee_fuse_masks_sha"] = sha(masks[ids].astype(bool))
+    out["room_ieee_fuse_depth"] = crops(fd)
     return os.path.join(out_dir, "ref_goldens_room.npz"), out
 
 
