@@ -49,6 +49,25 @@ def test_oracle_resize_properties():
     assert np.array_equal(up, np.repeat(np.repeat(np.arange(12).reshape(3, 4), 2, 0), 2, 1))
 
 
+def test_oracle_resize_matches_torch_bilinear():
+    """The restated INTER_LINEAR resize against torch's bilinear
+    interpolation with the same pixel-centre mapping (align_corners=False,
+    no antialiasing): within one grey level everywhere (the restatement
+    rounds 11-bit fixed-point weights, torch interpolates in float), which
+    pins the coordinate mapping and the border handling."""
+    import torch
+
+    rng = np.random.default_rng(6)
+    for (h, w), (oh, ow) in (((1200, 1600), (288, 384)), ((97, 131), (288, 384)), ((50, 61), (33, 47))):
+        img = rng.integers(0, 256, (h, w, 3)).astype(np.uint8)
+        ours = osp.resize_linear(img, oh, ow).astype(np.float64)
+        t = torch.from_numpy(img.astype(np.float64)).permute(2, 0, 1)[None]
+        ref = torch.nn.functional.interpolate(t, size=(oh, ow), mode="bilinear", align_corners=False,
+                                              antialias=False)[0].permute(1, 2, 0).numpy()
+        assert np.abs(ours - ref).max() <= 1.0, (h, w, np.abs(ours - ref).max())
+        assert np.abs(ours - ref).mean() <= 0.3
+
+
 def test_oracle_segments_are_connected_and_large_enough():
     bgr, _ = indoor_image(60, 80, 5)
     lab = osp.felzenszwalb(bgr, 100.0, 0.5, 20)
