@@ -582,6 +582,22 @@ __device__ void init_pixel(const DevView& V, const DevParams& prm, int px, int p
     }
 }
 
+// The source views a weighted sum visits, as a bit set walked in ascending
+// order (the accumulation order of the reference).  With the software
+// samplers each lane pair walks only its own selected views, so at step k
+// every pair of the warp evaluates its k-th selected view on the same
+// instructions instead of the warp stepping through every view with the
+// unselected pairs idle (geometric pass 6-9 % faster, results unchanged).
+// A texture fetch whose texture differs across the warp costs more than the
+// idle lanes save (random pass 5.5 % slower), so the texture sampler walks
+// every view and skips the unselected ones.
+__device__ __forceinline__ uint32_t all_view_bits(int N) { return N >= 32 ? 0xffffffffu : ((1u << N) - 1u); }
+template <class S>
+__device__ __forceinline__ uint32_t sel_views(uint32_t sel, int N) {
+    if constexpr (S::kTex) return all_view_bits(N);
+    else return sel;
+}
+
 // --------------------------------------------------------------- sweep --
 // One pixel of a half-sweep: CheckerboardPropagation (patch_match_kernel.cu:
 // 813-1351; gmvs/src/patch_match.cu:678-1041) then PlaneHypothesisRefinement
@@ -920,7 +936,9 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
                 const bool fk = (flags >> k) & 1u;
                 GeomPoint gk;
                 if (geom && fk) gk = geom_point(V, NPL(k), px, py);
-                for (int j = 0; j < N; ++j) {
+                // the views with a nonzero weight, ascending (see the hypothesis loop)
+                for (uint32_t todo = sel_views<S>(temp_sel, N); todo; todo &= todo - 1u) {
+                    const int j = __ffs(todo) - 1;
                     const float w = VW(j);
                     if (w > 0) {
                         if (geom && fk)
@@ -1052,7 +1070,8 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
         GeomPoint gp;
         if (geom && !all_views) gp = geom_point(V, pl, px, py);
         float acc = 0.0f;
-        for (int j = 0; j < N; ++j) {
+        for (uint32_t todo = all_views ? all_view_bits(N) : sel_views<S>(temp_sel, N); todo; todo &= todo - 1u) {
+            const int j = __ffs(todo) - 1;
             float w = 0.0f;
             if (!all_views) {
                 w = VW(j);
