@@ -582,6 +582,19 @@ __device__ void init_pixel(const DevView& V, const DevParams& prm, int px, int p
     }
 }
 
+// The geometric terms of source views ja and jb (jb < 0: none) for the
+// pixel of lane pair q: each lane evaluates one and a shuffle hands both
+// lanes both, instead of both lanes evaluating both.  Both lanes of the pair
+// call this with the same arguments, so the shuffle always has its partner.
+__device__ __forceinline__ void pair_geom(const DevView& V, int ja, int jb, const GeomPoint& g, int px, int py,
+                                          const Pair& q, float& ga, float& gb) {
+    const int jm = q.h ? jb : ja;
+    const float gm = jm >= 0 ? geom_cost(V, jm, g, px, py) : 0.0f;
+    const float go = __shfl_xor_sync(q.mask, gm, 1);
+    ga = q.h ? go : gm;
+    gb = q.h ? gm : go;
+}
+
 // The source views a weighted sum visits, as a bit set walked in ascending
 // order (the accumulation order of the reference).  With the software
 // samplers each lane pair walks only its own selected views, so at step k
@@ -937,14 +950,23 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
                 GeomPoint gk;
                 if (geom && fk) gk = geom_point(V, NPL(k), px, py);
                 // the views with a nonzero weight, ascending (see the hypothesis loop)
-                for (uint32_t todo = sel_views<S>(temp_sel, N); todo; todo &= todo - 1u) {
-                    const int j = __ffs(todo) - 1;
-                    const float w = VW(j);
-                    if (w > 0) {
-                        if (geom && fk)
-                            acc += w * (CA(k, j) + 0.1f * geom_cost(V, j, gk, px, py));
-                        else
-                            acc += w * CA(k, j);
+                if (geom && fk) {
+                    // two views a step, the geometric term of one on each lane of the pair
+                    for (uint32_t todo = temp_sel; todo;) {
+                        const int ja = __ffs(todo) - 1;
+                        todo &= todo - 1u;
+                        const int jb = todo ? __ffs(todo) - 1 : -1;
+                        if (jb >= 0) todo &= todo - 1u;
+                        float ga, gb;
+                        pair_geom(V, ja, jb, gk, px, py, q, ga, gb);
+                        acc += VW(ja) * (CA(k, ja) + 0.1f * ga);
+                        if (jb >= 0) acc += VW(jb) * (CA(k, jb) + 0.1f * gb);
+                    }
+                } else {
+                    for (uint32_t todo = sel_views<S>(temp_sel, N); todo; todo &= todo - 1u) {
+                        const int j = __ffs(todo) - 1;
+                        const float w = VW(j);
+                        if (w > 0) acc += w * CA(k, j);
                     }
                 }
                 FC(k) = acc / weight_norm;
@@ -1067,8 +1089,22 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
         // the hypothesis against every source view (neighbours) or the
         // sampled ones (current plane, refinement)
         const Hyp hy = make_hyp(rc, pl);
-        GeomPoint gp;
-        if (geom && !all_views) gp = geom_point(V, pl, px, py);
+        if (geom && !all_views) {
+            // the geometric terms of the selected views, split across the
+            // lane pair, parked in row 0 of the neighbour-cost matrix (no
+            // longer read once the eight final costs are formed at s == 8)
+            const GeomPoint gp = geom_point(V, pl, px, py);
+            for (uint32_t todo = temp_sel; todo;) {
+                const int ja = __ffs(todo) - 1;
+                todo &= todo - 1u;
+                const int jb = todo ? __ffs(todo) - 1 : -1;
+                if (jb >= 0) todo &= todo - 1u;
+                float ga, gb;
+                pair_geom(V, ja, jb, gp, px, py, q, ga, gb);
+                CA(0, ja) = ga;
+                if (jb >= 0) CA(0, jb) = gb;
+            }
+        }
         float acc = 0.0f;
         for (uint32_t todo = all_views ? all_view_bits(N) : sel_views<S>(temp_sel, N); todo; todo &= todo - 1u) {
             const int j = __ffs(todo) - 1;
@@ -1081,7 +1117,7 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
             if (all_views)
                 CA(s, j) = c;
             else if (geom)
-                acc += w * (c + 0.1f * geom_cost(V, j, gp, px, py));
+                acc += w * (c + 0.1f * CA(0, j));
             else
                 acc += w * c;
         }
