@@ -363,12 +363,18 @@ def serving_run(dev, rates=(0.5, 4.0), num_jobs: int = 3, seed: int = 5, views=(
         jobs = serving.poisson_stream(num_jobs, rate, seed=seed + k, sizes=sizes, views=views, src=src, device=dev)
         torch.cuda.synchronize()
         srv = serving.ReconstructionServer(device=dev, max_active=2, prior_threads=min(16, os.cpu_count() or 1))
+        refused = []
         for j in jobs:
-            srv.submit(j)
+            try:
+                srv.submit(j)
+            except ValueError:  # larger than the whole memory budget
+                refused.append(j)
+        jobs = [j for j in jobs if j not in refused]
         srv.run()
         srv.close()
         st = serving.latency_stats(jobs)
-        st.update({"jobs": len(jobs), "errors": sum(j.error is not None for j in jobs),
+        st.update({"jobs": len(jobs), "errors": sum(j.error is not None for j in jobs), "refused": len(refused),
+                   "single_kernel_geometric_jobs": sum(not srv.split_geom(j) for j in jobs),
                    "mix": [f"{j.num_views}x{j.images.shape[2]}x{j.images.shape[1]}" for j in jobs]})
         if plain:
             t0 = time.perf_counter()

@@ -25,6 +25,7 @@ import threading
 import time
 from concurrent.futures import Future, ThreadPoolExecutor
 from dataclasses import dataclass, field
+from types import SimpleNamespace
 from typing import Dict, List, Optional
 
 import numpy as np
@@ -34,10 +35,12 @@ from .pipeline import SceneInputs, ScenePipeline
 
 # Bytes per pixel of one view that ScenePipeline keeps on the device
 # (batched mode, worst-case staging):
-#   images fp32 4; depth/normal/cost/planes double-buffered 72; prior planes
-#   and masks 20; fused depth/normal 16; masks 1; texture staging of the
-#   random and prior passes 4 + 4; quad staging of each geometric pass 16.
-_PER_VIEW_BYTES = 4 + 72 + 20 + 16 + 1 + 8
+#   images fp32 4 (+ 1 for the 8-bit upload); depth/normal/cost/planes
+#   double-buffered 72; prior planes and masks 20; fused depth/normal 16;
+#   masks 1; texture staging of the random and prior passes, each run as
+#   two view-group plans that may both read every image, 2 x 2 x 4; quad
+#   staging of each geometric pass 16.
+_PER_VIEW_BYTES = 4 + 1 + 72 + 20 + 16 + 1 + 16
 _PER_GEOM_PASS_VIEW_BYTES = 16
 # per reference view and pass: plane/cost/view-mask ping-pong + converted planes
 _PER_REF_PASS_BYTES = 64
@@ -54,18 +57,24 @@ def _num_sms() -> int:
 
 
 def footprint_bytes(num_views: int, height: int, width: int, num_refs: int, geom_iters: int = 2,
-                    max_src: int = 32, sms: Optional[int] = None) -> int:
-    """Upper bound of the device memory one job holds while it is active."""
+                    max_src: int = 32, sms: Optional[int] = None, split_geom: bool = True) -> int:
+    """Upper bound of the device memory one job holds while it is active.
+    `split_geom`: the geometric passes run their half-sweeps as two kernels,
+    which pass each pixel's neighbour costs through a scratch as large as
+    all reference views of the pass; the random and prior passes of a served
+    job run single kernels."""
     px = height * width
     per_view = _PER_VIEW_BYTES + geom_iters * _PER_GEOM_PASS_VIEW_BYTES
     passes = 2 + geom_iters
-    pitch_slack = 2 * num_views * height * 256  # texture rows padded to 256 bytes
-    ca = passes * (sms or _num_sms()) * 64 * _CA_BYTES_PER_WARP_SRC * max_src
-    # split half-sweeps (an autotuner choice): per pass and reference view,
+    plans = 4 + geom_iters  # random and prior passes in two view groups each
+    pitch_slack = 4 * num_views * height * 256  # texture rows padded to 256 bytes
+    ca = plans * (sms or _num_sms()) * 64 * _CA_BYTES_PER_WARP_SRC * max_src
+    # split half-sweeps: per geometric pass and reference view,
     # (8 * max_src + 10) words for every pixel of one colour, tiles rounded up
-    split = passes * num_refs * (width + 16) * (height + 16) // 2 * (8 * max_src + 10) * 4
-    return (px * (num_views * per_view + num_refs * passes * _PER_REF_PASS_BYTES + 4) + pitch_slack + ca + split +
-            _FIXED_BYTES)
+    split = (geom_iters * num_refs * (width + 16) * (height + 16) // 2 * (8 * max_src + 10) * 4) if split_geom else 0
+    total = px * (num_views * per_view + num_refs * passes * _PER_REF_PASS_BYTES + 4) + pitch_slack + ca + split
+    # the caching allocator's rounding and fragmentation: 5 % on top
+    return total + total // 20 + _FIXED_BYTES
 
 
 @dataclass
@@ -111,10 +120,10 @@ class Job:
         if self.superpixels is not None and tuple(self.superpixels.shape) != tuple(self.images.shape):
             raise ValueError(f"job {self.job_id}: superpixels do not match the images")
 
-    def footprint(self, geom_iters: int) -> int:
+    def footprint(self, geom_iters: int, split_geom: bool = True) -> int:
         V, H, W = self.images.shape
         max_src = max((len(s) for _, s in self.problems), default=1)
-        return footprint_bytes(V, H, W, len(self.problems), geom_iters, max_src)
+        return footprint_bytes(V, H, W, len(self.problems), geom_iters, max_src, split_geom=split_geom)
 
 
 class Cancelled(RuntimeError):
@@ -167,11 +176,21 @@ class ReconstructionServer:
         return time.perf_counter() - self.t0
 
     # ----------------------------------------------------------- requests --
+    def split_geom(self, job: Job) -> bool:
+        """Whether the job's geometric half-sweeps run as two kernels (faster,
+        but their scratch grows with all the job's reference pixels): yes
+        while that footprint takes at most half the budget, so that a large
+        job does not shut every other job out; single kernels otherwise."""
+        return job.footprint(self.geom_iters, True) <= self.budget // 2
+
+    def _need(self, job: Job) -> int:
+        return job.footprint(self.geom_iters, self.split_geom(job))
+
     def submit(self, job: Job) -> Job:
         """Queue a job; it is admitted once it has arrived and fits."""
         job.validate()
-        if job.footprint(self.geom_iters) > self.budget:
-            raise ValueError(f"job {job.job_id} needs {job.footprint(self.geom_iters)} bytes, more than the "
+        if self._need(job) > self.budget:
+            raise ValueError(f"job {job.job_id} needs {self._need(job)} bytes, more than the "
                              f"server's whole budget of {self.budget}")
         with self._lock:
             heapq.heappush(self.queue, (job.arrival, job.job_id, job))
@@ -183,7 +202,7 @@ class ReconstructionServer:
             arrival, _, job = self.queue[0]
             if arrival > now:
                 return
-            need = job.footprint(self.geom_iters)
+            need = self._need(job)
             if self.in_use + need > self.budget:
                 return  # admission in arrival order: wait for memory
             heapq.heappop(self.queue)
@@ -214,8 +233,9 @@ class ReconstructionServer:
             imgs = host.pin_memory().to(self.device, non_blocking=True).to(torch.float32)
             scene = SceneInputs(images=imgs, cams=list(job.cams), problems=[(r, list(s)) for r, s in job.problems],
                                 superpixels=job.superpixels)
+            params = None if self.split_geom(job) else SimpleNamespace(split_sweep=0)
             pipe = ScenePipeline(scene, geom_iters=self.geom_iters, mode="batched",
-                                 prior_threads=self.prior_threads, graphs=self.graphs)
+                                 prior_threads=self.prior_threads, graphs=self.graphs, params=params)
         st.synchronize()
         pipe.prepare(st)
         job.admitted = self.now()

@@ -108,6 +108,21 @@ def test_slots_and_future_arrivals():
     srv.close()
 
 
+def test_large_jobs_run_single_kernel_geometric_half_sweeps():
+    """The split geometric half-sweeps' scratch grows with all of a job's
+    reference pixels; a job whose split footprint would take more than half
+    the budget runs single kernels and is admitted with the smaller footprint."""
+    job = _job(0)
+    split, single = job.footprint(2, True), job.footprint(2, False)
+    assert single < split
+    small = _StandIn(memory_budget=int(1.5 * split))
+    assert not small.split_geom(job) and small._need(job) == single
+    big = _StandIn(memory_budget=4 * split)
+    assert big.split_geom(job) and big._need(job) == split
+    small.close()
+    big.close()
+
+
 def test_oversized_job_is_refused():
     srv = _StandIn(memory_budget=1 << 20)
     with pytest.raises(ValueError):
