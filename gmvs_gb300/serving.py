@@ -205,8 +205,9 @@ class ReconstructionServer:
             need = self._need(job)
             if self.in_use + need > self.budget:
                 return  # admission in arrival order: wait for memory
+            if self._start(job, need) is False:
+                return  # the device is fuller than the accounting says: wait for a job to finish
             heapq.heappop(self.queue)
-            self._start(job, need)
 
     def cancel(self, job_id: int) -> bool:
         """Cancel a queued or active job; an active one stops at its next
@@ -226,21 +227,40 @@ class ReconstructionServer:
                 return True
         return False
 
-    def _start(self, job: Job, need: int) -> None:
+    def _start(self, job: Job, need: int) -> bool:
+        """Allocate the job's device state and plans; False (nothing kept)
+        when the device runs out of memory while other jobs are resident —
+        the caller retries once one of them has finished.  The job is then
+        accounted at the larger of its footprint bound and what it really
+        took."""
         st = self._free_streams.pop() if self._free_streams else torch.cuda.Stream(device=self.device)
-        with torch.cuda.stream(st):
-            host = torch.from_numpy(np.ascontiguousarray(job.images))
-            imgs = host.pin_memory().to(self.device, non_blocking=True).to(torch.float32)
-            scene = SceneInputs(images=imgs, cams=list(job.cams), problems=[(r, list(s)) for r, s in job.problems],
-                                superpixels=job.superpixels)
-            params = None if self.split_geom(job) else SimpleNamespace(split_sweep=0)
-            pipe = ScenePipeline(scene, geom_iters=self.geom_iters, mode="batched",
-                                 prior_threads=self.prior_threads, graphs=self.graphs, params=params)
-        st.synchronize()
-        pipe.prepare(st)
+        before = torch.cuda.memory_allocated(self.device)
+        pipe = None
+        try:
+            with torch.cuda.stream(st):
+                host = torch.from_numpy(np.ascontiguousarray(job.images))
+                imgs = host.pin_memory().to(self.device, non_blocking=True).to(torch.float32)
+                scene = SceneInputs(images=imgs, cams=list(job.cams),
+                                    problems=[(r, list(s)) for r, s in job.problems], superpixels=job.superpixels)
+                params = None if self.split_geom(job) else SimpleNamespace(split_sweep=0)
+                pipe = ScenePipeline(scene, geom_iters=self.geom_iters, mode="batched",
+                                     prior_threads=self.prior_threads, graphs=self.graphs, params=params)
+            st.synchronize()
+            pipe.prepare(st)
+        except torch.OutOfMemoryError:
+            if pipe is not None:
+                pipe.close()
+            pipe = scene = imgs = None
+            self._free_streams.append(st)
+            torch.cuda.empty_cache()
+            if not self.active:
+                raise
+            return False
         job.admitted = self.now()
+        need = max(need, torch.cuda.memory_allocated(self.device) - before)
         self.in_use += need
         self.active.append(_Active(job=job, pipe=pipe, stream=st, bytes=need))
+        return True
 
     # ------------------------------------------------------------ stepping --
     def _record(self, a: _Active) -> None:
