@@ -161,6 +161,18 @@ __device__ __forceinline__ void unit_tile(int u, int TH, int wide, int& t, int& 
     row = r >> 1;
     t = 2 * s + (r & 1);
 }
+// Drops a warp-private scratch block whose contents are dead from L2 without
+// writing it back to DRAM (PTX `discard.global.L2`, a weak write of an
+// indeterminate value to each 128-byte line).  `base` is 128-byte aligned and
+// `bytes` a multiple of 128.  The warp barriers order every lane's last reads
+// of the block before the discards and the discards before the next writes.
+__device__ __forceinline__ void discard_l2_block(const void* base, int bytes, unsigned lane) {
+    __syncwarp();
+    const size_t g = __cvta_generic_to_global(base);
+    for (int off = (int)lane * 128; off < bytes; off += 32 * 128)
+        asm volatile("discard.global.L2 [%0], 128;" ::"l"(g + (size_t)off) : "memory");
+    __syncwarp();
+}
 __device__ __forceinline__ int claim_unit(int* q, unsigned lane) {
     int u = 0;
     if (lane == 0) u = atomicAdd(q + 1, 1);
