@@ -10,7 +10,9 @@ images, 2.5 GB of per-view state) exceed L2, so no flush is needed.
 
 Beside the timed steps the line carries (rank 0): the reference's own plain
 per-view GPU path on the same scene (`reference_gpu`, its kernels compiled
-from its sources) and this build's plain per-view chain (`plain_path`); the
+from its sources), this build's plain per-view chain (`plain_path`) and the
+same reconstruction through the scene-level C ABI with host buffers
+(`e2e_job_api`); the
 fp16-staged NCC's error against the FP64 oracle (`precision`); the served
 streams of the serving form (`serving`) and the 64-view batching form
 (`batching_form`); the dominant kernel's roofline and issue figures; one
@@ -52,6 +54,8 @@ def parse():
     ap.add_argument("--height", type=int, default=1200)
     ap.add_argument("--width", type=int, default=1600)
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-view comparison step")
+    ap.add_argument("--no-job-api", action="store_true",
+                    help="skip the end-to-end run through the scene-level C ABI (e2e_job_api)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-serving", action="store_true", help="skip the served-stream latency measurement")
     ap.add_argument("--no-batching", action="store_true", help="skip the 64-view batching-form measurement")
@@ -275,6 +279,83 @@ def reference_gpu_run(sc, geom_iters: int = 2, gc: int = 3) -> dict:
 
 
 # -------------------------------------------------------------- precision --
+def job_api_run(inputs, pipe, host_images, steps: int = 3, geom_iters: int = 2, gc: int = 3) -> dict:
+    """The same reconstruction through the scene-level C ABI that a host in
+    another language binds (gmvs_ctx_create, gmvs_job_create,
+    gmvs_pass_random_prior, gmvs_pass_geom twice, gmvs_job_fuse, gmvs_export
+    into host arrays, gmvs_job_destroy), with host buffers: every step
+    uploads the fp32 images from pinned host memory, creates the job (its
+    device state included), runs the passes with the launch shapes the
+    pipeline's autotuner chose, fuses, exports every view's fused depth and
+    normals to pinned host arrays and destroys the job, all inside the
+    wall-clock timed region.  The fused depth maps are compared with the
+    batched pipeline's."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from gmvs_gb300 import _abi, engine
+
+    L = _abi.lib()
+    V, H, W = inputs.images.shape
+    dev_images = torch.empty((V, H, W), dtype=torch.float32, device=inputs.images.device)
+    cams = (_abi.gmvs_camera * V)(*inputs.cams)
+    probs = (_abi.gmvs_problem * len(inputs.problems))(*[engine.make_problem(r, s) for r, s in inputs.problems])
+    sp = np.ascontiguousarray(inputs.superpixels)
+    pr = engine.params_struct()
+    pg = engine.params_struct(max_iterations=2)
+    if "random0" in pipe.tuned:
+        pr = pipe.tuned["random0"].apply(pr)
+    if "geom0" in pipe.tuned:
+        pg = pipe.tuned["geom0"].apply(pg)
+    out_d = torch.empty((len(inputs.problems), H, W), dtype=torch.float32).pin_memory()
+    out_n = torch.empty((len(inputs.problems), H, W, 3), dtype=torch.float32).pin_memory()
+    ctx = ctypes.c_void_p()
+    if L.gmvs_ctx_create(torch.cuda.current_device(), ctypes.byref(ctx)) != 0:
+        raise RuntimeError("gmvs_ctx_create failed")
+
+    def check(rc):
+        if rc != 0:
+            buf = ctypes.create_string_buffer(512)
+            L.gmvs_ctx_last_error(ctx, buf, 512)
+            raise RuntimeError(buf.value.decode())
+
+    def step():
+        dev_images.copy_(host_images, non_blocking=True)
+        job = ctypes.c_void_p()
+        check(L.gmvs_job_create(ctx, cams, V, H, W, dev_images.data_ptr(), sp.ctypes.data, probs,
+                                len(inputs.problems), ctypes.byref(job)))
+        try:
+            check(L.gmvs_pass_random_prior(job, None, 0, ctypes.byref(pr), None))
+            for _ in range(geom_iters):
+                check(L.gmvs_pass_geom(job, None, 0, ctypes.byref(pg), None, None, None))
+            check(L.gmvs_job_fuse(job, None, 0, gc, None, None))
+            for i, (ref, _) in enumerate(inputs.problems):
+                check(L.gmvs_export(job, ref, 1, out_d[i].data_ptr(), out_n[i].data_ptr(), None, None))
+            torch.cuda.synchronize()
+        finally:
+            L.gmvs_job_destroy(job)
+
+    try:
+        step()  # warm-up (plans, module loading)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            step()
+        torch.cuda.synchronize()
+        s = (time.perf_counter() - t0) / steps
+    finally:
+        L.gmvs_ctx_destroy(ctx)
+    ref_ids = [r for r, _ in inputs.problems]
+    equal = bool(torch.equal(out_d, pipe.fused_depth[ref_ids].cpu()))
+    return {"value": len(inputs.problems) / s, "unit": UNIT, "steps": steps, "s_per_step": s,
+            "h2d_bytes_per_step": host_images.numel() * 4, "d2h_bytes_per_step": out_d.numel() * 4 + out_n.numel() * 4,
+            "fused_depth_equal_pipeline": equal,
+            "note": "scene-level C ABI with host buffers (images in, fused maps out), job created and destroyed "
+                    "every step, wall clock; no CUDA graphs and the host triangulation not overlapped"}
+
+
 def precision_run(sc, dev, pipe, plain_fused) -> dict:
     """Per-result error statement of the precision form: the fp16-staged
     NCC (texel quads, fp32 moments, FP64 homography constants) against the
@@ -701,6 +782,10 @@ def main():
     torch.cuda.synchronize()
     e2e_ms = e2.elapsed_time(e3) / args.steps
 
+    job_api = None
+    if not args.no_job_api and rank == 0:
+        job_api = job_api_run(inputs, pipe, torch.from_numpy(sc.images.astype("float32")).pin_memory())
+
     plain = pp_fused = None
     if not args.no_plain and rank == 0:
         pp = ScenePipeline(inputs, mode="plain", prior_threads=min(16, os.cpu_count() or 1))
@@ -787,8 +872,9 @@ def main():
                      "kernel": "k_sweep (half-sweep over all views)", "peak_source": peak_note,
                      "launch_ms": sweep_ms,
                      "traffic_note": "measured mean over the half-sweep launches of one step (ncu, one pass); "
-                                     "the excess over the algorithmic bytes is per-pixel scratch written back "
-                                     "from L2 (profiles/k_sweep_traffic_room_20views_1600x1200.json)",
+                                     "the excess over the algorithmic bytes is scratch written back from L2: "
+                                     "register spills and the split half-sweep's per-pixel matrices "
+                                     "(profiles/k_sweep_traffic_room_20views_1600x1200.json)",
                      "note": "latency-bound texture/L1 gather, not HBM: ncu shows 36-47 % SM issue, 37 % of the "
                              "texture pipe and under 2 % of DRAM bandwidth"},
         "ncc_samples": ncc_samples_block(samples, ms, clocks),
@@ -796,6 +882,7 @@ def main():
         "gpu_launches": launches * args.steps,
         "clocks": clocks,
         "plain_path": plain,
+        "e2e_job_api": job_api,
         "reference_gpu": ref_gpu,
         "speedup_vs_reference_gpu": ({"value": value / ref_gpu["value"],
                                       "e2e": world * args.views / (e2e_ms / 1000.0) / ref_gpu["value"],
