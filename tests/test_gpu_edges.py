@@ -156,3 +156,42 @@ def test_texture_arrays_equal_pitched_textures(gmvs_lib, orc, cuda):
             for t in (0, 1)]
     _check(outs[1], outs[0])
     _check(outs[1], _oracle_pass(orc, sc, ids, sampler=1, max_iterations=2))
+
+
+@pytest.mark.parametrize("num_src", [17, 32])
+def test_many_sources(gmvs_lib, orc, cuda, num_src):
+    """More than 16 source views (the second half of the view-selection draw
+    counters) up to the maximum, GMVS_MAX_NGB = 32 (every bit of the
+    selection masks, the widest neighbour-cost matrices): the random pass
+    with the texture sampler, and the geometric pass with fp16 texel quads
+    as one kernel and split in two, against the oracle bit for bit."""
+    sc = synthetic.room_scene(0, H=72, W=96, num_views=num_src + 1, device=cuda)
+    ids = list(range(num_src + 1))
+    dmin, dmax = sc.depth_range
+    p = engine.params_struct(sampler=_abi.SAMPLER_TEX, max_iterations=2)
+    v = gpu_view(sc, ids, cuda, dmin, dmax)
+    v.allocate_outputs(with_planes=True)
+    engine.run_passes([v], p, engine.Workspace())
+    g = (v.out_depth.cpu().numpy(), v.out_normal.cpu().numpy(), v.out_cost.cpu().numpy())
+    od, on, oc, _ = orc.run_pass(cam_args(sc, ids), sc.images[ids].astype(np.float32),
+                                 orc.make_params(sampler=1, depth_min=dmin, depth_max=dmax, stream_id=0,
+                                                 max_iterations=2))
+    _check(g, (od, on, oc))
+    assert (v.out_depth > 0).float().mean().item() > 0.5
+
+    rng = np.random.default_rng(4)
+    d = (sc.depths * (1.0 + rng.normal(0, 0.005, sc.depths.shape))).astype(np.float32)
+    n = sc.normals + rng.normal(0, 0.02, sc.normals.shape)
+    n = (n / np.linalg.norm(n, axis=-1, keepdims=True)).astype(np.float32)
+    op = orc.make_params(sampler=0, depth_min=dmin, depth_max=dmax, init_kind=2, sweep_kind=2, max_iterations=2,
+                         pass_index=2, stream_id=0)
+    o = orc.run_pass(cam_args(sc, ids), sc.images[ids].astype(np.float32), op, depths=d[ids], ref_normal=n[0])[:3]
+    for split in (0, 1):
+        p = engine.params_struct(sampler=_abi.SAMPLER_CLAMP, staging=_abi.STAGE_QUAD_F16,
+                                 init_kind=_abi.INIT_DEPTH_NORMAL, sweep_kind=_abi.SWEEP_GEOM, max_iterations=2,
+                                 pass_index=2, split_sweep=split)
+        v = gpu_view(sc, ids, cuda, dmin, dmax, depths=[torch.from_numpy(d[i]).to(cuda) for i in ids],
+                     ref_normal=torch.from_numpy(n[0]).to(cuda))
+        v.allocate_outputs(with_planes=True)
+        engine.run_passes([v], p, engine.Workspace())
+        _check((v.out_depth.cpu().numpy(), v.out_normal.cpu().numpy(), v.out_cost.cpu().numpy()), o)
