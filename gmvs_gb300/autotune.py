@@ -37,7 +37,7 @@ from .engine import Plan, ViewInputs, Workspace
 # (tile_w, tile_h) -> 16 x 8, 16 x 16, 32 x 8 and 32 x 16 pixel tiles
 TILE_SHAPES = ((16, 4), (16, 8), (32, 4), (32, 8))
 CTAS_PER_SM = (0,)
-SPLIT = (0, 1)
+SPLIT = (0, 1, 2)  # half-sweeps as one, two or three kernels
 # (tile_h, ctas_per_sm, split_sweep, tile_w); 2-row tiles and 1-3 CTAs per
 # SM never won a sweep on the room scene (fewer resident warps) and are left
 # out of the default list

@@ -77,6 +77,9 @@ struct DevParams {
     // thread row of a tile): nbc + u * 8 * nmax * 16, nbi + u * 10 * 16.
     float* nbc;
     int* nbi;
+    // Three-kernel half-sweeps: nbc holds a ninth row (the current plane's
+    // costs) and rfs + u * kRefineWords * 16 the refinement state.
+    float* rfs;
     int ca_slots;  // warp blocks in `ca`
     int nb_units;  // unit blocks in `nbc` / `nbi`
     int wide;      // 32-pixel-wide tiles: the tile list pairs 16-column tiles (see unit_tile)

@@ -23,19 +23,19 @@ struct LaunchShape {
 cudaError_t launch_init_f32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*, int*,
                             bool generic, cudaStream_t);
 cudaError_t launch_sweep_f32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*, int,
-                             int*, bool generic, bool split, cudaStream_t);
+                             int*, bool generic, int split, cudaStream_t);
 cudaError_t launch_init_qf32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*, int*,
                              bool generic, cudaStream_t);
 cudaError_t launch_sweep_qf32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*, int,
-                              int*, bool generic, bool split, cudaStream_t);
+                              int*, bool generic, int split, cudaStream_t);
 cudaError_t launch_init_qf16(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*, int*,
                              bool generic, cudaStream_t);
 cudaError_t launch_sweep_qf16(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*, int,
-                              int*, bool generic, bool split, cudaStream_t);
+                              int*, bool generic, int split, cudaStream_t);
 cudaError_t launch_init_tex(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*, int*,
                             bool generic, cudaStream_t);
 cudaError_t launch_sweep_tex(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*, int, int*,
-                             bool generic, bool split, cudaStream_t);
+                             bool generic, int split, cudaStream_t);
 // Per-pixel NCC cost matrix of given hypotheses (gmvs_ncc_costs).
 cudaError_t launch_ncc_f32(const LaunchShape&, const DevView*, const DevParams&, const Tile*, int*,
                            const float4*, float*, float*, uint32_t*, bool generic, cudaStream_t);

@@ -612,6 +612,13 @@ __device__ __forceinline__ uint32_t sel_views(uint32_t sel, int N) {
 }
 
 // --------------------------------------------------------------- sweep --
+// Per-pixel words the three-kernel half-sweep passes from its selection
+// kernel to its refinement kernel: current plane (4), its cost and depth,
+// selected views, the view-selection draw counters (4), the three
+// refinement planes (12), the random and perturbed depths, the depth before
+// refinement and the restricted cost; one spare.
+constexpr int kRefineWords = 28;
+
 // One pixel of a half-sweep: CheckerboardPropagation (patch_match_kernel.cu:
 // 813-1351; gmvs/src/patch_match.cu:678-1041) then PlaneHypothesisRefinement
 // (patch_match_kernel.cu:684-811; gmvs/src/patch_match.cu:595-676), by a lane
@@ -625,12 +632,19 @@ __device__ __forceinline__ uint32_t sel_views(uint32_t sel, int N) {
 // PH selects the part of the half-sweep: 0 = all of it; 1 = the neighbour
 // hypotheses only (their cost matrix and positions go to per-pixel scratch);
 // 2 = the rest, from that scratch.  1 then 2 compute exactly what 0 does, as
-// two kernels with fewer live registers each.  `nb` (PH > 0): this pixel's
-// 10 scratch words (flags, same-colour bits, 8 positions) at stride 16.
+// two kernels with fewer live registers each.  Three kernels: 3 = the
+// neighbour hypotheses and the current plane against every source view
+// (cost matrix rows 0-7 and row 8), 4 = view selection, the candidates' final
+// costs, the current plane's cost from row 8, the best candidate and the
+// refinement planes, with no NCC (state to `rf`), 5 = the five refinement
+// hypotheses, from `rf`.  3, 4, 5 compute exactly what 0 does.  `nb`
+// (PH 1-4): this pixel's 10 scratch words (flags, same-colour bits, 8
+// positions) at stride 16; `rf` (PH 4, 5): its kRefineWords state words at
+// stride 16.
 template <class S, int NS, int PH>
 __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int py, int iter, int colour, float* my,
                             int npix, const Pair& q, float2* pw, int pstride, float* __restrict__ ca,
-                            int* __restrict__ nb) {
+                            int* __restrict__ nb, float* __restrict__ rf) {
     const int W = V.W, H = V.H, N = V.N, nmax = prm.nmax;
     const int center = py * W + px;
     const int same = iter & 1;
@@ -654,12 +668,14 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
         P.pw = pw;
         P.pstride = pstride;
     }
-    make_patch<S, NS>(P, S(V, 0), V, prm, px, py, q);
+    if constexpr (PH != 4) make_patch<S, NS>(P, S(V, 0), V, prm, px, py, q);  // PH 4 runs no NCC
 
     // Adaptive checkerboard sampling.  pos = linear index; the buffer of a
     // candidate follows from its offset parity (odd = other colour).
     unsigned flags = 0u, fromsame = 0u;
-    if constexpr (PH == 2) {
+    if constexpr (PH == 5) {
+        // the refinement needs no neighbour positions
+    } else if constexpr (PH == 2 || PH == 4) {
         flags = (unsigned)nb[0];
         fromsame = (unsigned)nb[16];
         for (int k = 0; k < 8; ++k)
@@ -847,7 +863,7 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
         }
         for (int k = 0; k < 8; ++k)
             if ((flags >> k) & 1u) POS(k) = pos[k];
-        if constexpr (PH == 1) {
+        if constexpr (PH == 1 || PH == 3) {
             if (q.h == 0) {
                 nb[0] = (int)flags;
                 nb[16] = (int)fromsame;
@@ -868,9 +884,39 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
     const bool use_prior = prior_mode && mask > 0;
     int min_idx = 0;
 
-    for (int s = PH == 2 ? 8 : 0; s < (PH == 1 ? 8 : 14); ++s) {
+    if constexpr (PH == 5) {
+        // the state the selection kernel left (layout: kRefineWords)
+        cur = make_float4(rf[0], rf[16], rf[32], rf[48]);
+        cur_cost = rf[4 * 16];
+        depth_now = rf[5 * 16];
+        cur_sel = __float_as_uint(rf[6 * 16]);
+        const unsigned long long cnt_lo = (unsigned long long)__float_as_uint(rf[7 * 16]) |
+                                          ((unsigned long long)__float_as_uint(rf[8 * 16]) << 32);
+        const unsigned long long cnt_hi = (unsigned long long)__float_as_uint(rf[9 * 16]) |
+                                          ((unsigned long long)__float_as_uint(rf[10 * 16]) << 32);
+        for (int i = 0; i < N; ++i) {  // the selection kernel's weights, in its order
+            const float w = (float)((((i < 16) ? cnt_lo : cnt_hi) >> ((i & 15) * 4)) & 15ull);
+            VW(i) = w;
+            if (w > 0) {
+                temp_sel |= 1u << i;
+                weight_norm += w;
+            }
+        }
+        for (int c = 0; c < 12; ++c) PL4(c >> 2, c & 3) = rf[(11 + c) * 16];
+        depth_rand = rf[23 * 16];
+        depth_pert = rf[24 * 16];
+        dnow = rf[25 * 16];
+        restricted_cost = rf[26 * 16];
+        if (prior_mode) {
+            ppl = V.prior_planes[center];
+            depth_prior = depth_from_plane(rc, ppl, px, py);
+        }
+    }
+    constexpr int s_begin = (PH == 2 || PH == 4) ? 8 : (PH == 5 ? 9 : 0);
+    constexpr int s_end = PH == 1 ? 8 : (PH == 3 ? 9 : (PH == 4 ? 10 : 14));
+    for (int s = s_begin; s < s_end; ++s) {
         float4 pl;
-        const bool all_views = s < 8;
+        const bool all_views = s < 8 || PH == 3;
         if (s < 8) {
             if (!((flags >> s) & 1u)) {
                 // the reference's `float cost_array[8][32] = {2.0f}` (2 at [0][0], else 0)
@@ -878,6 +924,8 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
                 continue;
             }
             pl = NPL(s);
+        } else if (PH == 3) {
+            pl = cur;  // its costs against every view: row 8 of the matrix
         } else if (s == 8) {
             // multi-hypothesis joint view selection (patch_match_kernel.cu:1114-1176)
             const uint32_t* so = V.sel[opp];
@@ -942,6 +990,14 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
                     weight_norm += w;
                 }
             }
+            if constexpr (PH == 4) {
+                if (q.h == 0) {
+                    rf[7 * 16] = __uint_as_float((uint32_t)cnt_lo);
+                    rf[8 * 16] = __uint_as_float((uint32_t)(cnt_lo >> 32));
+                    rf[9 * 16] = __uint_as_float((uint32_t)cnt_hi);
+                    rf[10 * 16] = __uint_as_float((uint32_t)(cnt_hi >> 32));
+                }
+            }
             // final costs of the 8 candidates (patch_match_kernel.cu:1178-1211;
             // gmvs/src/patch_match.cu:920-946)
             for (int k = 0; k < 8; ++k) {
@@ -981,7 +1037,7 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
             }
             pl = cur;
         } else {
-            if (s == 9) {
+            if (s == 9 && PH != 5) {
                 cur_cost = cost_now;
                 depth_now = depth_from_plane(rc, cur, px, py);
                 if (prior_mode) {
@@ -1077,6 +1133,20 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
                 PL4(1, 0) = n_rand.x, PL4(1, 1) = n_rand.y, PL4(1, 2) = n_rand.z, PL4(1, 3) = n_rand.w;
                 PL4(2, 0) = n_pert.x, PL4(2, 1) = n_pert.y, PL4(2, 2) = n_pert.z, PL4(2, 3) = n_pert.w;
                 dnow = depth_now;
+                if constexpr (PH == 4) {
+                    if (q.h == 0) {
+                        rf[0] = cur.x, rf[16] = cur.y, rf[32] = cur.z, rf[48] = cur.w;
+                        rf[4 * 16] = cur_cost;
+                        rf[5 * 16] = depth_now;
+                        rf[6 * 16] = __uint_as_float(cur_sel);
+                        for (int c = 0; c < 12; ++c) rf[(11 + c) * 16] = PL4(c >> 2, c & 3);
+                        rf[23 * 16] = depth_rand;
+                        rf[24 * 16] = depth_pert;
+                        rf[25 * 16] = dnow;
+                        rf[26 * 16] = restricted_cost;
+                    }
+                    return;
+                }
             }
             // candidates (depth, normal): (rand, base), (now, rand), (rand, rand), (now, pert), (pert, base)
             const int k = s - 9;
@@ -1088,7 +1158,8 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
 
         // the hypothesis against every source view (neighbours) or the
         // sampled ones (current plane, refinement)
-        const Hyp hy = make_hyp(rc, pl);
+        Hyp hy{};
+        if constexpr (PH != 4) hy = make_hyp(rc, pl);
         if (geom && !all_views) {
             // the geometric terms of the selected views, split across the
             // lane pair, parked in row 0 of the neighbour-cost matrix (no
@@ -1113,7 +1184,11 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
                 w = VW(j);
                 if (!(w > 0)) continue;
             }
-            const float c = ncc_cost<S, NS>(V, prm, j, hy, P, px, py, q);
+            float c;
+            if constexpr (PH == 4)
+                c = CA(8, j);  // the current plane's cost, from the first kernel
+            else
+                c = ncc_cost<S, NS>(V, prm, j, hy, P, px, py, q);
             if (all_views)
                 CA(s, j) = c;
             else if (geom)
@@ -1122,7 +1197,7 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
                 acc += w * c;
         }
         if (s == 8) {
-            cost_now = acc / weight_norm;
+            if constexpr (PH != 3) cost_now = acc / weight_norm;
         } else if (s > 8) {
             const float tc = acc / weight_norm;
             const float db = depth_from_plane(rc, pl, px, py);
@@ -1143,7 +1218,7 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
             }
         }
     }
-    if (PH != 1 && q.h == 0) {
+    if ((PH == 0 || PH == 2 || PH == 5) && q.h == 0) {
         V.plane[outb][center] = cur;
         V.cost[outb][center] = cur_cost;
         V.sel[outb][center] = cur_sel;

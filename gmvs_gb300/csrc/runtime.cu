@@ -165,6 +165,7 @@ struct Layout {
     size_t state = 0;
     size_t ca = 0;         // neighbour-cost scratch of the resident warps
     size_t nbc = 0, nbi = 0;  // split half-sweeps: per-unit neighbour costs and positions
+    size_t rfs = 0;           // three-kernel half-sweeps: per-unit refinement state
     int ca_ctas = 0;       // resident CTAs per SM it holds
     size_t total = 0;
     int ntiles = 0;
@@ -225,7 +226,7 @@ int32_t validate(const gmvs_view_pass* views, int32_t n, const gmvs_params* p) {
     if (p->tile_w != 0 && p->tile_w != 16 && p->tile_w != 32)
         return fail(GMVS_ERR_INVALID, "tile_w must be 0, 16 or 32");
     if (p->ctas_per_sm < 0 || p->ctas_per_sm > 32) return fail(GMVS_ERR_INVALID, "ctas_per_sm must be in [0, 32]");
-    if (p->split_sweep != 0 && p->split_sweep != 1) return fail(GMVS_ERR_INVALID, "split_sweep must be 0 or 1");
+    if (p->split_sweep < 0 || p->split_sweep > 2) return fail(GMVS_ERR_INVALID, "split_sweep must be 0, 1 or 2");
     if (p->tex_storage != 0 && p->tex_storage != 1) return fail(GMVS_ERR_INVALID, "tex_storage must be 0 or 1");
     for (int v = 0; v < n; ++v) {
         const gmvs_view_pass& V = views[v];
@@ -339,11 +340,18 @@ Layout make_layout(const gmvs_view_pass* views, int32_t n, const gmvs_params* p,
         const size_t warps = (size_t)num_sms() * L.ca_ctas * tile_h_of(p);
         off = align_up(off + warps * 16 * 8 * nmax * sizeof(float));
         if (p->split_sweep) {
+            // the three-kernel form keeps a ninth row (the current plane's
+            // costs) and the refinement state
             const size_t units = (size_t)ntiles * tile_h_of(p);
+            const size_t rows = p->split_sweep == 2 ? 9 : 8;
             L.nbc = off;
-            off = align_up(off + units * 16 * 8 * nmax * sizeof(float));
+            off = align_up(off + units * 16 * rows * nmax * sizeof(float));
             L.nbi = off;
             off = align_up(off + units * 16 * 10 * sizeof(int));
+            if (p->split_sweep == 2) {
+                L.rfs = off;
+                off = align_up(off + units * 16 * kRefineWords * sizeof(float));
+            }
         }
     }
     L.total = off;
@@ -455,7 +463,7 @@ struct gmvs_plan {
     DevParams dprm;
     int variant = 0;
     bool generic = false;
-    bool split = false;   // half-sweeps as two kernels (gmvs_params.split_sweep)
+    int split = 0;        // half-sweeps as one, two or three kernels (gmvs_params.split_sweep)
     char* ws = nullptr;
     int* d_err = nullptr;
     int* d_ntiles = nullptr;  // tile queue: count, next unit, warps done
@@ -569,9 +577,10 @@ int32_t build_plan(gmvs_plan* P, const gmvs_view_pass* views, int32_t n, const g
         if (p->split_sweep) {
             P->dprm.nbc = (float*)(P->ws + L.nbc);
             P->dprm.nbi = (int*)(P->ws + L.nbi);
+            if (p->split_sweep == 2) P->dprm.rfs = (float*)(P->ws + L.rfs);
         }
     }
-    P->split = with_state && p->split_sweep != 0;
+    P->split = with_state ? p->split_sweep : 0;
     P->slots = L.slots;
     int32_t rc = create_textures(P, L);
     if (rc != GMVS_OK) return rc;

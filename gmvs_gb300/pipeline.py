@@ -150,9 +150,9 @@ class ScenePipeline:
         if self.base is not None and kind == "geom" and hasattr(self.base, "geom_max_iterations"):
             p.max_iterations = self.base.geom_max_iterations
         if kind == "geom" and self.mode == "batched" and not hasattr(self.base, "split_sweep"):
-            # the fp16-quad geometric half-sweeps are faster as two kernels
+            # the fp16-quad geometric half-sweeps are faster as three kernels
             # (same results); the autotuner, when given, decides instead
-            p.split_sweep = 1
+            p.split_sweep = 2
         return p
 
     def _passes(self):

@@ -59,10 +59,10 @@ def _num_sms() -> int:
 def footprint_bytes(num_views: int, height: int, width: int, num_refs: int, geom_iters: int = 2,
                     max_src: int = 32, sms: Optional[int] = None, split_geom: bool = True) -> int:
     """Upper bound of the device memory one job holds while it is active.
-    `split_geom`: the geometric passes run their half-sweeps as two kernels,
-    which pass each pixel's neighbour costs through a scratch as large as
-    all reference views of the pass; the random and prior passes of a served
-    job run single kernels."""
+    `split_geom`: the geometric passes run their half-sweeps as three
+    kernels, which pass each pixel's neighbour costs and refinement state
+    through a scratch as large as all reference views of the pass; the
+    random and prior passes of a served job run single kernels."""
     px = height * width
     per_view = _PER_VIEW_BYTES + geom_iters * _PER_GEOM_PASS_VIEW_BYTES
     passes = 2 + geom_iters
@@ -70,8 +70,9 @@ def footprint_bytes(num_views: int, height: int, width: int, num_refs: int, geom
     pitch_slack = 4 * num_views * height * 256  # texture rows padded to 256 bytes
     ca = plans * (sms or _num_sms()) * 64 * _CA_BYTES_PER_WARP_SRC * max_src
     # split half-sweeps: per geometric pass and reference view,
-    # (8 * max_src + 10) words for every pixel of one colour, tiles rounded up
-    split = (geom_iters * num_refs * (width + 16) * (height + 16) // 2 * (8 * max_src + 10) * 4) if split_geom else 0
+    # (9 * max_src + 10 + 28) words for every pixel of one colour (cost
+    # matrix, neighbour positions, refinement state), tiles rounded up
+    split = (geom_iters * num_refs * (width + 16) * (height + 16) // 2 * (9 * max_src + 38) * 4) if split_geom else 0
     total = px * (num_views * per_view + num_refs * passes * _PER_REF_PASS_BYTES + 4) + pitch_slack + ca + split
     # the caching allocator's rounding and fragmentation: 5 % on top
     return total + total // 20 + _FIXED_BYTES
@@ -177,7 +178,7 @@ class ReconstructionServer:
 
     # ----------------------------------------------------------- requests --
     def split_geom(self, job: Job) -> bool:
-        """Whether the job's geometric half-sweeps run as two kernels (faster,
+        """Whether the job's geometric half-sweeps run as three kernels (faster,
         but their scratch grows with all the job's reference pixels): yes
         while that footprint takes at most half the budget, so that a large
         job does not shut every other job out; single kernels otherwise."""

@@ -140,11 +140,11 @@ class PatchMatcher:
             cams=[self.cameras_host[i] for i in ids], images=[imgs[i] for i in ids],
             depth_min=self.params.depth_min, depth_max=self.params.depth_max, stream_id=ref,
             depths=[deps[i] for i in ids], ref_normal=nrms[ref])
-        # the geometric half-sweeps run as two kernels unless the caller's
+        # the geometric half-sweeps run as three kernels unless the caller's
         # parameters say otherwise (same results, faster on the GB300)
         p = params_struct(self.params, init_kind=_abi.INIT_DEPTH_NORMAL, sweep_kind=_abi.SWEEP_GEOM,
                           sampler=_abi.SAMPLER_CLAMP, run_filter=1, pass_index=2,
-                          split_sweep=int(getattr(self.params, "split_sweep", 1)))
+                          split_sweep=int(getattr(self.params, "split_sweep", 2)))
         if self._ws is None:
             self._ws = Workspace()
         run_passes([v], p, self._ws)

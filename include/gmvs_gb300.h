@@ -121,7 +121,9 @@ typedef struct gmvs_params {
                                  leave more of the SM's L1 to the texture/sample cache */
     int32_t split_sweep;      /* 1 = each half-sweep as two kernels (neighbour hypotheses, then view
                                  selection and refinement) through a per-pixel scratch in the workspace;
-                                 same results */
+                                 2 = as three (neighbour hypotheses and the current plane, then view
+                                 selection and the refinement planes, then the refinement); same
+                                 results */
     int32_t tex_storage;      /* TEX sampler: 0 = pitched rows in the workspace; 1 = CUDA arrays (the
                                  block-linear layout module A uses), allocated by gmvs_plan_create and
                                  freed by gmvs_plan_destroy -- the one case where the library allocates

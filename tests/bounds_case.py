@@ -25,12 +25,16 @@ def cases(cuda):
         runs = {
             "tex": dict(sampler=_abi.SAMPLER_TEX, max_iterations=2),
             "tex_split": dict(sampler=_abi.SAMPLER_TEX, max_iterations=2, split_sweep=1),
+            "tex_split3": dict(sampler=_abi.SAMPLER_TEX, max_iterations=2, split_sweep=2),
             "f32": dict(sampler=_abi.SAMPLER_CLAMP, staging=_abi.STAGE_F32, max_iterations=2),
             "generic": dict(sampler=_abi.SAMPLER_CLAMP, staging=_abi.STAGE_QUAD_F16, patch_size=7,
                             radius_increment=1, max_iterations=1),
             "geom_split": dict(sampler=_abi.SAMPLER_CLAMP, staging=_abi.STAGE_QUAD_F16,
                                init_kind=_abi.INIT_DEPTH_NORMAL, sweep_kind=_abi.SWEEP_GEOM, max_iterations=2,
                                pass_index=2, split_sweep=1),
+            "geom_split3": dict(sampler=_abi.SAMPLER_CLAMP, staging=_abi.STAGE_QUAD_F16,
+                                init_kind=_abi.INIT_DEPTH_NORMAL, sweep_kind=_abi.SWEEP_GEOM, max_iterations=2,
+                                pass_index=2, split_sweep=2),
         }
         for key, kw in runs.items():
             extra = {}

@@ -10,9 +10,9 @@ from gmvs_gb300 import _abi, autotune
 
 
 def test_candidates_cover_tile_shapes_and_split():
-    # 16x8, 16x16, 32x8 and 32x16 pixel tiles, single and split half-sweeps
+    # 16x8, 16x16, 32x8 and 32x16 pixel tiles, half-sweeps as one, two or three kernels
     assert {(c[3], 2 * c[0]) for c in autotune.CANDIDATES} == {(16, 8), (16, 16), (32, 8), (32, 16)}
-    assert {c[2] for c in autotune.CANDIDATES} == {0, 1}
+    assert {c[2] for c in autotune.CANDIDATES} == {0, 1, 2}
     p = autotune.TuneResult("k", (4, 0, 1, 32)).apply(_abi.default_params())
     assert (p.tile_h, p.ctas_per_sm, p.split_sweep, p.tile_w) == (4, 0, 1, 32)
 

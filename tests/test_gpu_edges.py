@@ -9,7 +9,7 @@ import pytest
 import torch
 
 from gmvs_gb300 import _abi, engine, synthetic
-from scenes import cam_args, gpu_view
+from scenes import cam_args, gpu_view, gt_planes
 from test_gpu_parity import diff_report, same_bits
 
 pytestmark = pytest.mark.gpu
@@ -116,35 +116,49 @@ def test_staging_modes_agree(gmvs_lib, cuda, scene):
         _check(o, outs[0])
 
 
-@pytest.mark.parametrize("kind", ["random", "geom"])
+@pytest.mark.parametrize("kind", ["random", "prior", "geom"])
 def test_split_half_sweeps_equal_single_kernel(gmvs_lib, cuda, kind):
-    """A half-sweep as two kernels (neighbour hypotheses, then the rest)
-    computes exactly what the single kernel does."""
+    """A half-sweep as two kernels (neighbour hypotheses, then the rest) or
+    three (neighbour hypotheses and the current plane, then view selection
+    and the refinement planes, then the refinement) computes exactly what
+    the single kernel does."""
     sc = synthetic.small_scene(0, H=128, W=160)
     views = [sc.problems[0], sc.problems[1]]
     rng = np.random.default_rng(3)
     d = (sc.depths * (1.0 + rng.normal(0, 0.005, sc.depths.shape))).astype(np.float32)
     n = sc.normals + rng.normal(0, 0.02, sc.normals.shape)
     n = (n / np.linalg.norm(n, axis=-1, keepdims=True)).astype(np.float32)
+    prior = {}
+    if kind == "prior":
+        # a prior over every pixel: the restricted-cost branches everywhere
+        t = lambda a, dt=torch.float32: torch.from_numpy(np.ascontiguousarray(a)).to(device=cuda, dtype=dt)
+        for ref, _ in views:
+            pl = gt_planes(sc, ref)
+            prior[ref] = dict(prior_planes=t(pl), prior_masks=t(np.full(pl.shape[:2], 1, np.int32), torch.int32),
+                              init_planes=t(pl), init_costs=t(np.full(pl.shape[:2], 0.5, np.float32)))
     outs = []
-    for split in (0, 1):
+    for split in (0, 1, 2):
         if kind == "random":
             p = engine.params_struct(sampler=_abi.SAMPLER_TEX, max_iterations=3, split_sweep=split)
+        elif kind == "prior":
+            p = engine.params_struct(sampler=_abi.SAMPLER_TEX, init_kind=_abi.INIT_PRIOR, sweep_kind=_abi.SWEEP_PRIOR,
+                                     pass_index=1, split_sweep=split)
         else:
             p = engine.params_struct(sampler=_abi.SAMPLER_CLAMP, init_kind=_abi.INIT_DEPTH_NORMAL,
                                      sweep_kind=_abi.SWEEP_GEOM, max_iterations=2, pass_index=2, split_sweep=split)
         vs = []
         for ref, src in views:
             ids = [ref] + list(src)
-            extra = {} if kind == "random" else dict(depths=[torch.from_numpy(d[i]).to(cuda) for i in ids],
-                                                      ref_normal=torch.from_numpy(n[ref]).to(cuda))
+            extra = {"random": {}, "prior": prior.get(ref, {})}.get(kind) if kind != "geom" else dict(
+                depths=[torch.from_numpy(d[i]).to(cuda) for i in ids], ref_normal=torch.from_numpy(n[ref]).to(cuda))
             v = gpu_view(sc, ids, cuda, 0.3, 6.0, **extra)
             v.allocate_outputs(with_planes=True)
             vs.append(v)
         engine.run_passes(vs, p, engine.Workspace())
         outs.append([(v.out_depth.cpu().numpy(), v.out_normal.cpu().numpy(), v.out_cost.cpu().numpy()) for v in vs])
-    for a, b in zip(outs[0], outs[1]):
-        _check(b, a)
+    for split in (1, 2):
+        for a, b in zip(outs[0], outs[split]):
+            _check(b, a)
 
 
 def test_texture_arrays_equal_pitched_textures(gmvs_lib, orc, cuda):
