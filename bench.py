@@ -944,7 +944,7 @@ def sweep_roofline(pipe, torch):
                     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                     a.record(stream)
                 plan.launch_stage(s)
-                launches += 2 if (is_sweep and plan.params.split_sweep) else 1  # split: two kernels
+                launches += (1 + plan.params.split_sweep) if is_sweep else 1  # split: two or three kernels
                 if is_sweep:
                     b.record(stream)
                     durations.append((a, b))
