@@ -624,9 +624,10 @@ constexpr int kRefineWords = 28;
 // (patch_match_kernel.cu:684-811; gmvs/src/patch_match.cu:595-676), by a lane
 // pair.  Reads the state at the start of the half-sweep (buffer `same` for
 // this colour, `opp` for the other) and writes the pixel to buffer `outb`.
-// `my` is the pixel's shared-memory slot (stride npix): the 8 x nmax cost
-// matrix, nmax view weights, then the cold per-pixel state (neighbour
-// positions, candidate final costs, refinement planes).  All 14 hypotheses
+// `my` is the pixel's shared-memory slot (stride npix): nmax view weights,
+// then the cold per-pixel state (neighbour positions, candidate final costs,
+// refinement planes); the 8 x nmax cost matrix (9 x nmax in the three-kernel
+// form) is `ca`, global scratch at stride 16.  All 14 hypotheses
 // (8 neighbours, the current plane, 5 refinement candidates) go through one
 // NCC loop.
 // PH selects the part of the half-sweep: 0 = all of it; 1 = the neighbour
