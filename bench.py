@@ -875,8 +875,10 @@ def main():
                                      "the excess over the algorithmic bytes is scratch written back from L2: "
                                      "register spills and the split half-sweep's per-pixel matrices "
                                      "(profiles/k_sweep_traffic_room_20views_1600x1200.json)",
-                     "note": "latency-bound texture/L1 gather, not HBM: ncu shows 36-47 % SM issue, 37 % of the "
-                             "texture pipe and under 2 % of DRAM bandwidth"},
+                     "note": "bound by the L1/texture unit, not HBM: ncu shows the texture half-sweep at 75 % of "
+                             "L1TEX throughput (L1-to-L2 requests busy 74 % of cycles) and 41 % SM issue, the "
+                             "three-kernel geometric half-sweep at 53-69 % SM issue, all under 7 % of DRAM "
+                             "bandwidth"},
         "ncc_samples": ncc_samples_block(samples, ms, clocks),
         "stages_s": stages,
         "gpu_launches": launches * args.steps,
