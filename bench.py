@@ -353,7 +353,8 @@ def job_api_run(inputs, pipe, host_images, steps: int = 3, geom_iters: int = 2, 
             "h2d_bytes_per_step": host_images.numel() * 4, "d2h_bytes_per_step": out_d.numel() * 4 + out_n.numel() * 4,
             "fused_depth_equal_pipeline": equal,
             "note": "scene-level C ABI with host buffers (images in, fused maps out), job created and destroyed "
-                    "every step, wall clock; no CUDA graphs and the host triangulation not overlapped"}
+                    "every step, wall clock; no CUDA graphs, the host triangulation of one view group overlapping "
+                    "the other's device work"}
 
 
 def precision_run(sc, dev, pipe, plain_fused) -> dict:

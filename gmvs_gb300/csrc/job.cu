@@ -47,6 +47,8 @@ struct gmvs_job {
     int geom_count = 0;
     void* ws = nullptr;  // plan workspace, grown on demand
     size_t ws_bytes = 0;
+    void* ws2 = nullptr;  // the second view group's, for the random + prior pass
+    size_t ws2_bytes = 0;
     void* fuse_scratch = nullptr;
     size_t fuse_bytes = 0;
 };
@@ -276,53 +278,30 @@ extern "C" void gmvs_job_destroy(gmvs_job* job) {
     DeviceGuard dg(job->ctx->device);
     cudaDeviceSynchronize();
     if (job->ws) cudaFree(job->ws);
+    if (job->ws2) cudaFree(job->ws2);
     if (job->fuse_scratch) cudaFree(job->fuse_scratch);
     if (job->block) cudaFree(job->block);
     delete job;
 }
 
-extern "C" int32_t gmvs_pass_random_prior(gmvs_job* job, const int32_t* problem_ids, int32_t n,
-                                          const gmvs_params* params, void* stream) {
-    const char* who = "gmvs_pass_random_prior";
-    if (!job || !params) return fail(GMVS_ERR_INVALID, std::string(who) + ": NULL");
-    DeviceGuard dg(job->ctx->device);
-    cudaStream_t st = (cudaStream_t)stream;
-    std::vector<int> set;
-    int32_t rc = problem_set(job, problem_ids, n, set, who);
-    if (rc != GMVS_OK) return job_fail(job, rc);
+namespace gmvs {
+namespace {
+
+// The planar prior of the given problems' reference views from their
+// first-pass depth and cost (host, all cores; planar_init.py:173-181).
+int32_t triangulate(const gmvs_job* job, const std::vector<int>& ids, const std::vector<float>& depth,
+                    const std::vector<float>& cost, std::vector<float>& planes, std::vector<uint32_t>& masks) {
     const size_t hw = (size_t)job->H * job->W;
-    // 1. random-initialisation pass (planar_init.py:113-172) into buffer 0
-    gmvs_params p = *params;
-    p.init_kind = GMVS_INIT_RANDOM;
-    p.sweep_kind = GMVS_SWEEP_PHOTO;
-    p.sampler = GMVS_SAMPLER_TEX;
-    p.pass_index = 0;
-    p.run_filter = 1;
-    std::vector<gmvs_view_pass> views;
-    for (int k : set) views.push_back(base_view(job, job->problems[k], 0));
-    rc = run_views(job, views, p, st, who);
-    if (rc != GMVS_OK) return job_fail(job, rc);
-    // 2. triangulation of every reference view on the host (planar_init.py:173-181)
-    std::vector<float> depth(set.size() * hw), cost(set.size() * hw), planes(set.size() * hw * 4);
-    std::vector<uint32_t> masks(set.size() * hw);
-    cudaError_t e = cudaSuccess;
-    for (size_t i = 0; i < set.size() && e == cudaSuccess; ++i) {
-        const int ref = job->problems[set[i]].ref_image_id;
-        e = cudaMemcpyAsync(depth.data() + i * hw, job->depth[0] + ref * hw, hw * 4, cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(cost.data() + i * hw, job->cost[0] + ref * hw, hw * 4, cudaMemcpyDeviceToHost, st);
-    }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return job_fail(job, fail_cuda(e, who));
     const bool spf = !job->superpixels.empty();
-    std::vector<int32_t> rcs(set.size(), GMVS_OK);
-    std::vector<std::string> errs(set.size());
-    const size_t nthreads = std::max<size_t>(1, std::min<size_t>(set.size(), std::max(1u, std::thread::hardware_concurrency())));
+    std::vector<int32_t> rcs(ids.size(), GMVS_OK);
+    std::vector<std::string> errs(ids.size());
+    const size_t nthreads =
+        std::max<size_t>(1, std::min<size_t>(ids.size(), std::max(1u, std::thread::hardware_concurrency())));
     std::vector<std::thread> pool;
     for (size_t t = 0; t < nthreads; ++t)
         pool.emplace_back([&, t]() {
-            for (size_t i = t; i < set.size(); i += nthreads) {
-                const int ref = job->problems[set[i]].ref_image_id;
+            for (size_t i = t; i < ids.size(); i += nthreads) {
+                const int ref = job->problems[ids[i]].ref_image_id;
                 float dmin, dmax;
                 view_range(job->cams[ref], dmin, dmax);
                 rcs[i] = gmvs_build_planar_prior(&job->cams[ref], job->H, job->W, depth.data() + i * hw,
@@ -334,39 +313,137 @@ extern "C" int32_t gmvs_pass_random_prior(gmvs_job* job, const int32_t* problem_
             }
         });
     for (auto& th : pool) th.join();
-    for (size_t i = 0; i < set.size(); ++i)
-        if (rcs[i] != GMVS_OK) return job_fail(job, fail(rcs[i], errs[i]));
-    for (size_t i = 0; i < set.size() && e == cudaSuccess; ++i) {
-        const int ref = job->problems[set[i]].ref_image_id;
-        e = cudaMemcpyAsync(job->prior_planes + ref * hw * 4, planes.data() + i * hw * 4, hw * 16,
-                            cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(job->prior_masks + ref * hw, masks.data() + i * hw, hw * 4, cudaMemcpyHostToDevice,
-                                st);
-    }
-    if (e != cudaSuccess) return job_fail(job, fail_cuda(e, who));
-    // 3. planar-prior pass (planar_init.py:181-190) from buffer 0 into buffer 1
-    p.init_kind = GMVS_INIT_PRIOR;
-    p.sweep_kind = GMVS_SWEEP_PRIOR;
-    p.pass_index = 1;
-    views.clear();
-    for (int k : set) {
-        gmvs_view_pass v = base_view(job, job->problems[k], 1);
-        const int ref = job->problems[k].ref_image_id;
-        v.prior_planes = job->prior_planes + ref * hw * 4;
-        v.prior_masks = job->prior_masks + ref * hw;
-        v.init_planes = job->planes[0] + ref * hw * 4;
-        v.init_costs = job->cost[0] + ref * hw;
-        views.push_back(v);
-    }
-    rc = run_views(job, views, p, st, who);
-    if (rc != GMVS_OK) return job_fail(job, rc);
-    // the host buffers above must outlive the uploads: they are pageable, so
-    // each upload returned once staged; synchronise anyway before they go
-    e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return job_fail(job, fail_cuda(e, who));
-    job->latest = 1;
+    for (size_t i = 0; i < ids.size(); ++i)
+        if (rcs[i] != GMVS_OK) return fail(rcs[i], errs[i]);
     return GMVS_OK;
+}
+
+}  // namespace
+}  // namespace gmvs
+
+// The problems run in two view groups so that the host triangulation of one
+// overlaps device work of the other: random pass of group 0, random pass of
+// group 1 (triangulation of group 0 meanwhile), prior pass of group 0
+// (triangulation of group 1 meanwhile), prior pass of group 1 -- the order
+// the Python pipeline uses.  A view's results do not depend on the grouping
+// (its random stream is keyed by its own id).  Each group's plans live in
+// their own workspace; plan descriptors are uploaded on a side stream so
+// that creating a plan does not wait for the other group's kernels.
+extern "C" int32_t gmvs_pass_random_prior(gmvs_job* job, const int32_t* problem_ids, int32_t n,
+                                          const gmvs_params* params, void* stream) {
+    const char* who = "gmvs_pass_random_prior";
+    if (!job || !params) return fail(GMVS_ERR_INVALID, std::string(who) + ": NULL");
+    DeviceGuard dg(job->ctx->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<int> set;
+    int32_t rc = problem_set(job, problem_ids, n, set, who);
+    if (rc != GMVS_OK) return job_fail(job, rc);
+    const size_t hw = (size_t)job->H * job->W;
+    // the random-initialisation pass (planar_init.py:113-172) into buffer 0,
+    // the planar-prior pass (planar_init.py:181-190) from buffer 0 into 1
+    gmvs_params pr = *params;
+    pr.init_kind = GMVS_INIT_RANDOM;
+    pr.sweep_kind = GMVS_SWEEP_PHOTO;
+    pr.sampler = GMVS_SAMPLER_TEX;
+    pr.pass_index = 0;
+    pr.run_filter = 1;
+    gmvs_params pp = pr;
+    pp.init_kind = GMVS_INIT_PRIOR;
+    pp.sweep_kind = GMVS_SWEEP_PRIOR;
+    pp.pass_index = 1;
+    const size_t G = set.size() >= 2 ? 2 : 1;
+    std::vector<int> grp[2];
+    for (size_t i = 0; i < set.size(); ++i) grp[i * G / set.size()].push_back(set[i]);
+    std::vector<gmvs_view_pass> rv[2], pv[2];
+    void** ws[2] = {&job->ws, &job->ws2};
+    size_t* ws_bytes[2] = {&job->ws_bytes, &job->ws2_bytes};
+    for (size_t g = 0; g < G; ++g) {
+        for (int k : grp[g]) {
+            rv[g].push_back(base_view(job, job->problems[k], 0));
+            gmvs_view_pass v = base_view(job, job->problems[k], 1);
+            const int ref = job->problems[k].ref_image_id;
+            v.prior_planes = job->prior_planes + ref * hw * 4;
+            v.prior_masks = job->prior_masks + ref * hw;
+            v.init_planes = job->planes[0] + ref * hw * 4;
+            v.init_costs = job->cost[0] + ref * hw;
+            pv[g].push_back(v);
+        }
+        const size_t nr = gmvs_plan_workspace_bytes(rv[g].data(), (int32_t)rv[g].size(), &pr);
+        const size_t np = gmvs_plan_workspace_bytes(pv[g].data(), (int32_t)pv[g].size(), &pp);
+        if (nr == 0 || np == 0) return job_fail(job, GMVS_ERR_INVALID);  // the message is set
+        rc = grow(ws[g], ws_bytes[g], std::max(nr, np), st, who);
+        if (rc != GMVS_OK) return job_fail(job, rc);
+    }
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    gmvs_plan* plan[2] = {nullptr, nullptr};
+    // on every exit: nothing of this call may still run when its plans,
+    // events, stream and host buffers go
+    auto finish = [&](int32_t code) {
+        cudaStreamSynchronize(st);
+        if (side) cudaStreamSynchronize(side);
+        for (size_t g = 0; g < 2; ++g) {
+            if (plan[g]) gmvs_plan_destroy(plan[g]);
+            if (ev[g]) cudaEventDestroy(ev[g]);
+        }
+        if (side) cudaStreamDestroy(side);
+        return job_fail(job, code);
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+    for (size_t g = 0; g < G && e == cudaSuccess; ++g) e = cudaEventCreateWithFlags(&ev[g], cudaEventDisableTiming);
+    if (e != cudaSuccess) return finish(fail_cuda(e, who));
+    // 1. both groups' random passes
+    for (size_t g = 0; g < G; ++g) {
+        rc = gmvs_plan_create(rv[g].data(), (int32_t)rv[g].size(), &pr, *ws[g], *ws_bytes[g], side, &plan[g]);
+        if (rc == GMVS_OK) rc = gmvs_plan_launch(plan[g], st);
+        if (rc != GMVS_OK) return finish(rc);
+        e = cudaEventRecord(ev[g], st);
+        if (e != cudaSuccess) return finish(fail_cuda(e, who));
+    }
+    for (size_t g = 0; g < G; ++g) {
+        // 2. group g's first-pass depth and cost to the host once its random
+        // pass is done, its triangulation there while the device runs on
+        const size_t m = grp[g].size();
+        std::vector<float> depth(m * hw), cost(m * hw), planes(m * hw * 4);
+        std::vector<uint32_t> masks(m * hw);
+        e = cudaStreamWaitEvent(side, ev[g], 0);
+        for (size_t i = 0; i < m && e == cudaSuccess; ++i) {
+            const int ref = job->problems[grp[g][i]].ref_image_id;
+            e = cudaMemcpyAsync(depth.data() + i * hw, job->depth[0] + ref * hw, hw * 4, cudaMemcpyDeviceToHost,
+                                side);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(cost.data() + i * hw, job->cost[0] + ref * hw, hw * 4, cudaMemcpyDeviceToHost,
+                                    side);
+        }
+        if (e != cudaSuccess) return finish(fail_cuda(e, who));
+        rc = gmvs_plan_check(plan[g], side);  // synchronises the side stream
+        if (rc != GMVS_OK) return finish(rc);
+        gmvs_plan_destroy(plan[g]);
+        plan[g] = nullptr;
+        rc = triangulate(job, grp[g], depth, cost, planes, masks);
+        if (rc != GMVS_OK) return finish(rc);
+        for (size_t i = 0; i < m && e == cudaSuccess; ++i) {
+            const int ref = job->problems[grp[g][i]].ref_image_id;
+            e = cudaMemcpyAsync(job->prior_planes + ref * hw * 4, planes.data() + i * hw * 4, hw * 16,
+                                cudaMemcpyHostToDevice, side);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(job->prior_masks + ref * hw, masks.data() + i * hw, hw * 4,
+                                    cudaMemcpyHostToDevice, side);
+        }
+        if (e != cudaSuccess) return finish(fail_cuda(e, who));
+        // 3. group g's prior pass; creating its plan synchronises the side
+        // stream, so the uploads above are done before it is queued
+        rc = gmvs_plan_create(pv[g].data(), (int32_t)pv[g].size(), &pp, *ws[g], *ws_bytes[g], side, &plan[g]);
+        if (rc == GMVS_OK) rc = gmvs_plan_launch(plan[g], st);
+        if (rc != GMVS_OK) return finish(rc);
+    }
+    for (size_t g = 0; g < G; ++g) {
+        rc = gmvs_plan_check(plan[g], st);
+        if (rc != GMVS_OK) return finish(rc);
+    }
+    rc = finish(GMVS_OK);
+    if (rc == GMVS_OK) job->latest = 1;
+    return rc;
 }
 
 extern "C" int32_t gmvs_pass_geom(gmvs_job* job, const int32_t* problem_ids, int32_t n, const gmvs_params* params,
