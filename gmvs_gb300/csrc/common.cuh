@@ -226,7 +226,7 @@ __device__ __forceinline__ float bilinear_clamp(const float* __restrict__ img, f
     const float wd = u - (float)wl;
     const int hu = (hl == H - 1) ? hl : hl + 1;
     const int wu = (wl == W - 1) ? wl : wl + 1;
-    const int n = H * W;
+    [[maybe_unused]] const int n = H * W;  // read by the bounds-checked build
     const float v0 = __ldg(img + GMVS_IDX(hl * W + wl, n, kOobDepth));
     const float v1 = __ldg(img + GMVS_IDX(hl * W + wu, n, kOobDepth));
     const float v2 = __ldg(img + GMVS_IDX(hu * W + wl, n, kOobDepth));

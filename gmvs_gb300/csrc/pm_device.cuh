@@ -930,7 +930,7 @@ __device__ void sweep_pixel(const DevView& V, const DevParams& prm, int px, int 
         } else if (s == 8) {
             // multi-hypothesis joint view selection (patch_match_kernel.cu:1114-1176)
             const uint32_t* so = V.sel[opp];
-            const int HW = H * W;
+            [[maybe_unused]] const int HW = H * W;  // read by the bounds-checked build
             const uint32_t nb_sel[4] = {(flags & 1u) ? so[GMVS_IDX(center - W, HW, kOobNeighbour)] : 0u,
                                         (flags & 4u) ? so[GMVS_IDX(center + W, HW, kOobNeighbour)] : 0u,
                                         (flags & 16u) ? so[GMVS_IDX(center - 1, HW, kOobNeighbour)] : 0u,
