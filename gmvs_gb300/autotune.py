@@ -45,6 +45,28 @@ CANDIDATES: Tuple[Tuple[int, ...], ...] = tuple(
     (th, c, sp, tw) for tw, th in TILE_SHAPES for c in CTAS_PER_SM for sp in SPLIT)
 
 
+# Candidates timed within this fraction of the fastest are ties (run-to-run
+# noise on a sample of the views).
+TIE = 0.005
+
+
+def pick(ms: Dict[str, float]) -> str:
+    """The fastest candidate; among ties the taller tile (fewer tiles and
+    queue claims), then the 16-pixel width, then fewer kernels per
+    half-sweep.  Tuned on a few views the tile shapes tie, while on the whole
+    64-view batching mix 16 x 16 tiles ran 4 % faster than 16 x 8."""
+    fastest = min(ms.values())
+    near = [k for k, v in ms.items() if v <= fastest * (1.0 + TIE)]
+
+    def rank(k: str):
+        c = [int(x) for x in k.split(",")]
+        th, sp = c[0], c[2] if len(c) > 2 else 0
+        tw = (c[3] if len(c) > 3 else 0) or 16
+        return (th, -tw, -sp, -ms[k])
+
+    return max(near, key=rank)
+
+
 def _copy_params(p: _abi.gmvs_params) -> _abi.gmvs_params:
     q = _abi.gmvs_params()
     ctypes.memmove(ctypes.byref(q), ctypes.byref(p), ctypes.sizeof(p))
@@ -124,7 +146,7 @@ class Autotuner:
                 ms[",".join(str(x) for x in (th, c, sp, tw)[:max(3, len(cand))])] = e0.elapsed_time(e1) / self.reps
             finally:
                 plan.close()
-        best = min(ms, key=ms.get)
+        best = pick(ms)
         res = TuneResult(key, tuple(int(x) for x in best.split(",")), ms)
         self.cache[key] = res
         self._save()

@@ -66,3 +66,10 @@ def test_tuner_picks_a_candidate(gmvs_lib, small, cuda):
     r = t.tune([v], engine.params_struct())
     assert r.best in ((4, 0, 0), (8, 0, 1), (2, 3, 0)) and len(r.ms) == 3 and all(ms > 0 for ms in r.ms.values())
     assert t.tune([v], engine.params_struct()) is r  # cached
+
+
+def test_pick_breaks_ties_toward_taller_narrower_tiles():
+    ms = {"4,0,0,16": 947.3, "4,0,1,16": 985.7, "8,0,0,16": 948.0, "4,0,0,32": 948.6, "8,0,0,32": 948.2}
+    assert autotune.pick(ms) == "8,0,0,16"  # all four single-kernel shapes tie within 0.5 %
+    assert autotune.pick({"4,0,2,16": 800.0, "8,0,2,16": 812.0, "8,0,0,16": 1160.0}) == "4,0,2,16"  # no tie
+    assert autotune.pick({"8,0,1,16": 100.0, "8,0,2,16": 100.2}) == "8,0,1,16"  # tie: fewer kernels
