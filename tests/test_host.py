@@ -161,3 +161,19 @@ def test_scene_files_use_reference_layout(tmp_path, small):
     assert _read_pairs(str(tmp_path / "pair.txt")) == small.problems
     assert np.array_equal(imageio.imread_gray(str(tmp_path / "images" / "0003.jpg")), small.images[3])
     assert np.load(str(tmp_path / "superpixels" / "0001.npy")).dtype == np.uint8
+
+
+def test_launch_parameters_are_validated_on_the_host(gmvs_lib):
+    """gmvs_plan_workspace_bytes rejects launch parameters out of range before
+    any CUDA call (0 bytes and a message): the half-sweep split (0, 1 or 2
+    kernels after the first), the tile width and the tile height."""
+    import ctypes
+
+    view = (_abi.gmvs_view_pass * 1)()
+    for field, value, words in (("split_sweep", 3, b"split_sweep must be 0, 1 or 2"),
+                                ("tile_w", 24, b"tile_w must be 0, 16 or 32"),
+                                ("tile_h", 9, b"tile_h must be in [0, 8]")):
+        p = _abi.default_params()
+        setattr(p, field, value)
+        assert gmvs_lib.gmvs_plan_workspace_bytes(view, 1, ctypes.byref(p)) == 0
+        assert words in gmvs_lib.gmvs_last_error()
